@@ -1,0 +1,171 @@
+/*
+ * kvtomo.h -- C ABI of the GB300 tomosynthesis projector / reconstruction engine.
+ *
+ * Every entry point is plain C: opaque handles, POD structs, raw pointers and
+ * sizes, a kv_status return code.  Nothing here exits the process; a failing
+ * call returns a status and kv_ctx_last_error() gives the message.
+ *
+ * Reference interfaces replaced (paths inside the Kevernals project):
+ *   kv_forward        <- Projector::PerformProjection(ImageDataPtr)
+ *                        source/modules/reconstruction/Projector.cu:873-1036
+ *                        (kernel CudaPerformProjection, Projector.cu:227-372)
+ *   kv_forward_single <- Projector::PerformProjection(volume, Position3D, container)
+ *                        Projector.cu:823-870 (left unfinished in the reference)
+ *   kv_back           <- Projector::PerformBackProjection(ImageDataPtr)
+ *                        Projector.cu:1038-1207 (kernel Projector.cu:376-785),
+ *                        recons::BackProjection Reconstructors.h:256-261
+ *   kv_sart           <- recons::ART      Reconstructors.h:19-134
+ *   kv_mlem           <- recons::MLEM     Reconstructors.h:136-253
+ *   kv_shift_and_add  <- recons::ShiftAndAdd Reconstructors.h:263-379
+ *   kv_geometry       <- the arrays Projector.cu:917-940 flattens out of
+ *                        TomoGeometry (TomoGeometry.h:34-89)
+ *   kv_uniform_volume <- PhantomMaker(volume, 1.f).GetPhantom(), the uniform
+ *                        start of ART/MLEM (Reconstructors.h:35-36, 152-153)
+ * Entry points without a reference counterpart (sensitivity image, FP64
+ * residual reductions, batched solves) say so beside their declaration.
+ *
+ * Conventions
+ *   Frame: volume-centred, as in the reference (TomoGeometry.cpp:127,162,330).
+ *   Volume: float32 [nz][ny][nx], x fastest; voxel (i,j,k) spans
+ *           [-nx*dx/2 + i*dx, -nx*dx/2 + (i+1)*dx] (same for y, z).
+ *   Projections: float32 [n_views][nv][nu], u fastest; pixel (u,v) of view p
+ *           has its centre at det_origin[p] + ((u+0.5)*du, (v+0.5)*dv, 0).
+ *   Memory: each data call takes a kv_mem flag.  KV_MEM_HOST: the library
+ *           copies in and out (pinned staging, stream-ordered, synchronous on
+ *           return).  KV_MEM_DEVICE: pointers are device memory of the
+ *           context's device; the call is asynchronous on the context stream.
+ *           The library never frees caller memory.
+ *   Threading: one kv_ctx per host thread; calls on a context are ordered on
+ *           its stream.
+ */
+#ifndef KVTOMO_H
+#define KVTOMO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KV_ABI_VERSION 1
+
+typedef enum kv_status {
+    KV_OK = 0,
+    KV_ERR_INVALID_ARG = 1, /* null pointer, size out of range, bad enum          */
+    KV_ERR_GEOMETRY = 2,    /* geometry the chosen operator family cannot express  */
+    KV_ERR_OOM = 3,         /* device or pinned host allocation failed             */
+    KV_ERR_CUDA = 4,        /* a CUDA runtime call failed                          */
+    KV_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up                  */
+    KV_ERR_NUMERIC = 6,     /* non-finite input or result                          */
+    KV_ERR_UNSUPPORTED = 7, /* operation not defined for this family / storage     */
+    KV_ERR_NO_DEVICE = 8    /* no CUDA device, or the device is not sm_103         */
+} kv_status;
+
+/* Operator family.
+ * KV_FAMILY_RC reproduces the reference kernels, quirks included: the forward
+ *   value of a ray is the path-length weighted MEAN of the voxels it crosses
+ *   (Projector.cu:348-371) and the backprojection is the voxel-driven,
+ *   11x11-window, weight-normalised operator (Projector.cu:452-776).
+ * KV_FAMILY_EXACT is the Siddon line integral A (mm * value) and its exact
+ *   transpose A^T; it needs the detector plane below the volume and every
+ *   source above it (the linear-sweep tomosynthesis geometry). */
+typedef enum kv_family { KV_FAMILY_RC = 0, KV_FAMILY_EXACT = 1 } kv_family;
+
+/* Storage type of the volume and projections while a solve runs on the
+ * device.  Arithmetic is FP32 in every case; the API buffers stay float32. */
+typedef enum kv_storage { KV_STORAGE_F32 = 0, KV_STORAGE_BF16 = 1, KV_STORAGE_F16 = 2 } kv_storage;
+
+typedef enum kv_mem { KV_MEM_HOST = 0, KV_MEM_DEVICE = 1 } kv_mem;
+
+typedef struct kv_geometry {
+    int32_t nx, ny, nz;       /* volume size in voxels                                  */
+    float dx, dy, dz;         /* voxel spacing (mm)                                     */
+    int32_t n_views;          /* number of projections                                  */
+    int32_t nu, nv;           /* detector ROI size in pixels                            */
+    float du, dv;             /* detector pixel spacing (mm)                            */
+    const float *src;         /* [n_views][3] source positions                          */
+    const float *det_origin;  /* [n_views][3] ROI bottom-left corner; z = detector plane */
+    float fulcrum_z;          /* shift-and-add focal height (TomoGeometry::fulcrum().z)   */
+} kv_geometry;
+
+typedef struct kv_ctx kv_ctx;
+typedef struct kv_plan kv_plan;
+
+/* Per-iteration callback of the iterative drivers.  residual is
+ * ||A x - p||_2 / ||p||_2 of the iterate entering the iteration and loglik the
+ * Poisson log-likelihood sum(p log(Ax) - Ax), both reduced in FP64; they are
+ * only computed when a callback is given.  Return nonzero to stop early. */
+typedef int (*kv_iter_cb)(int iteration, double residual, double loglik, void *user);
+
+/* ---- library / context ------------------------------------------------ */
+const char *kv_version(void);
+const char *kv_status_string(kv_status s);
+kv_status kv_ctx_create(int device, kv_ctx **out);
+kv_status kv_ctx_destroy(kv_ctx *ctx);
+/* Use `stream` (a cudaStream_t of the context's device, or NULL for the
+ * context's own stream) for every later call on this context. */
+kv_status kv_ctx_set_stream(kv_ctx *ctx, void *cuda_stream);
+kv_status kv_sync(kv_ctx *ctx);
+const char *kv_ctx_last_error(const kv_ctx *ctx);
+
+/* ---- plans -------------------------------------------------------------- */
+/* Validates the geometry, uploads per-view tables, and keeps the workspace a
+ * solve needs.  The geometry arrays are copied; the caller may free them. */
+kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *geom, kv_family family,
+                         kv_storage storage, kv_plan **out);
+kv_status kv_plan_destroy(kv_plan *plan);
+/* Number of elements of the volume and of the projection stack. */
+size_t kv_plan_volume_elems(const kv_plan *plan);
+size_t kv_plan_proj_elems(const kv_plan *plan);
+
+/* ---- operators ---------------------------------------------------------- */
+kv_status kv_forward(kv_plan *plan, const float *volume, float *projections, kv_mem mem);
+/* Forward projection of one view (source position and detector origin given
+ * explicitly) into an nv x nu container; completes Projector.cu:823-870. */
+kv_status kv_forward_single(kv_plan *plan, const float *volume, const float src[3],
+                            const float det_origin[3], float *projection, kv_mem mem);
+kv_status kv_back(kv_plan *plan, const float *projections, float *volume, kv_mem mem);
+/* Sensitivity image A^T 1, accumulated in FP64 (EXACT only).  No reference
+ * counterpart: the reference MLEM normalises inside its backprojector. */
+kv_status kv_sensitivity(kv_plan *plan, double *sens, kv_mem mem);
+/* Shift-and-add tomosynthesis: [nz][nv][nu] slices, one per volume slice, the
+ * detector ROI size as in the reference.  RC uses the reference's shift rule
+ * literally (Reconstructors.h:308-331); EXACT measures heights from the
+ * detector plane and shifts in detector pixels. */
+kv_status kv_shift_and_add(kv_plan *plan, const float *projections, float *slices, kv_mem mem);
+/* Host-only: the integer row shift of every (slice, view) pair that
+ * kv_shift_and_add applies, [nz][n_views], computed without a device.
+ * Replaces the shift loop of recons::ShiftAndAdd, Reconstructors.h:308-331. */
+kv_status kv_shift_and_add_shifts(const kv_geometry *geom, kv_family family, int32_t *shifts);
+/* Fill `volume` with the uniform initial estimate 1.0 (PhantomMaker(vol,1.f)). */
+kv_status kv_uniform_volume(kv_plan *plan, float *volume, kv_mem mem);
+
+/* Rasterises a sum of ellipsoids, sampled at voxel centres, into a volume of
+ * nx*ny*nz voxels centred at the origin.  params holds n rows of 16 floats:
+ * centre[3], semi-axes[3], M[9] (row-major, local coordinates = M (q - c)),
+ * density.  Used to generate seeded phantoms for the benchmarks and the
+ * warm-start training data.  No reference counterpart: the reference phantom
+ * (PhantomMaker.cpp:9-51) has boxes and spheres sampled at voxel corners. */
+kv_status kv_phantom_ellipsoids(kv_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, float dx, float dy,
+                                float dz, const float *params, int32_t n, float *volume, kv_mem mem);
+
+/* ---- iterative drivers -------------------------------------------------- */
+/* MLEM.  RC: q = A x; where q != 0, q <- relax * p / q; x <- x * B(q), the
+ * reference semantics.  EXACT: x <- x * A^T(relax * p / A x) / A^T 1.  The
+ * volume is updated in place, as the reference does with its initial volume. */
+kv_status kv_mlem(kv_plan *plan, const float *projections, float *volume_inout, int iterations,
+                  float relax, kv_mem mem, kv_iter_cb cb, void *user);
+/* Simultaneous ART.  RC: x <- x + B(relax * (p - A x)) (recons::ART).  EXACT:
+ * SART, x <- x + relax * C A^T(R (p - A x)), R = 1/(A 1), C = 1/(A^T 1). */
+kv_status kv_sart(kv_plan *plan, const float *projections, float *volume_inout, int iterations,
+                  float relax, kv_mem mem, kv_iter_cb cb, void *user);
+/* ||A x - p||_2 / ||p||_2 and sum(p log(Ax) - Ax) reduced in FP64.  No
+ * reference counterpart (the reference has no stopping criterion). */
+kv_status kv_residual(kv_plan *plan, const float *projections, const float *volume, kv_mem mem,
+                      double *rel_residual, double *loglik);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KVTOMO_H */

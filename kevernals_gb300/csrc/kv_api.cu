@@ -1,0 +1,552 @@
+// kv_api.cu -- the C ABI (include/kvtomo.h): contexts, plans, operators and
+// the iterative drivers.  Host code only; the kernels live in kv_exact.cu,
+// kv_rc.cu and kv_misc.cu.
+#include "kv_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+
+kv_status kv_fail(kv_ctx *ctx, kv_status s, const char *fmt, ...) {
+    if (ctx != nullptr) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return s;
+}
+
+namespace {
+
+// Reduction helpers (kv_reduce.cu)
+kv_status residual_from_red(kv_ctx *ctx, double *res, double *ll) {
+    double h[3];
+    KV_CHECK_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_red, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (res) *res = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+    if (ll) *ll = h[2];
+    return KV_OK;
+}
+
+template <typename T>
+kv_status ensure(kv_ctx *ctx, T **p, size_t bytes) {
+    if (*p == nullptr) KV_CHECK_CUDA(ctx, cudaMalloc((void **)p, bytes));
+    return KV_OK;
+}
+
+// Resolves a caller float buffer to a device pointer: device memory is used
+// as is; host memory goes through a plan workspace buffer (copied in when
+// `copy_in`).
+kv_status stage_in(kv_plan *plan, const float *user, kv_mem mem, float **staging, size_t n,
+                   bool copy_in, float **dev) {
+    if (mem == KV_MEM_DEVICE) {
+        *dev = const_cast<float *>(user);
+        return KV_OK;
+    }
+    KV_TRY(ensure(plan->ctx, staging, n * sizeof(float)));
+    if (copy_in)
+        KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(*staging, user, n * sizeof(float), cudaMemcpyHostToDevice,
+                                                 plan->ctx->stream));
+    *dev = *staging;
+    return KV_OK;
+}
+
+kv_status stage_out(kv_plan *plan, float *user, kv_mem mem, const float *dev, size_t n) {
+    if (mem == KV_MEM_DEVICE) return KV_OK;
+    KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(user, dev, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                             plan->ctx->stream));
+    KV_CHECK_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
+    return KV_OK;
+}
+
+kv_status check_common(kv_plan *plan, const void *a, const void *b, kv_mem mem) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (a == nullptr || b == nullptr) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "null buffer");
+    if (mem != KV_MEM_HOST && mem != KV_MEM_DEVICE) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad kv_mem");
+    KV_CHECK_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+    return KV_OK;
+}
+
+kv_status ensure_sens(kv_plan *plan) {
+    if (plan->sens_valid) return KV_OK;
+    KV_TRY(ensure(plan->ctx, &plan->d_sens, plan->nvox * sizeof(double)));
+    KV_TRY(exact_sensitivity_launch(plan, plan->d_sens));
+    plan->sens_valid = true;
+    return KV_OK;
+}
+
+// Integer row shifts of shift-and-add, one per (slice, view).
+// rule RC follows recons::ShiftAndAdd literally (Reconstructors.h:287-331);
+// rule EXACT uses heights above the detector plane and detector pixels.
+kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_t *sh) {
+    const int P = g.n_views, nz = g.nz;
+    if (nz <= 1) return kv_fail(ctx, KV_ERR_GEOMETRY, "shift-and-add needs at least 2 slices (got %d)", nz);
+    if (P <= 1) return kv_fail(ctx, KV_ERR_GEOMETRY, "shift-and-add needs at least 2 projections (got %d)", P);
+    // common source z (TomoTable: float mean) and detector z (double sum, float mean)
+    float src_z = 0.f;
+    for (int i = 0; i < P; ++i) src_z += g.src[3 * i + 2];
+    src_z /= (float)P;
+    double acc = 0.0;
+    for (int i = 0; i < P; ++i) acc += g.det_origin[3 * i + 2];
+    const float det_z = (float)acc / (float)P;
+    auto almost_equal = [](float a, float b) {
+        float d = std::fabs(a - b), fa = std::fabs(a), fb = std::fabs(b);
+        return d <= 1.1920928955078125e-07f * (fa > fb ? fa : fb);
+    };
+    if (family == KV_FAMILY_RC) {
+        const float sid = std::fabs(det_z - src_z);
+        const float zf = g.fulcrum_z;
+        if (almost_equal(zf, sid)) return kv_fail(ctx, KV_ERR_GEOMETRY, "fulcrum at the source height");
+        const float mf = sid / (sid - zf);
+        const float wz = (float)nz * g.dz;
+        float z = (float)(-0.5 * (double)wz);
+        for (int k = 0; k < nz; ++k) {
+            if (k > 0) z = z + g.dz;
+            if (almost_equal(z, sid)) return kv_fail(ctx, KV_ERR_GEOMETRY, "slice %d at the source height", k);
+            const float coeff = sid / (sid - z) - mf;
+            for (int i = 0; i < P; ++i) {
+                const float t = g.src[3 * i + 1] * coeff;
+                sh[(size_t)k * P + i] = (int32_t)(t / g.dy);
+            }
+        }
+    } else {
+        const double sid = (double)src_z - (double)det_z;
+        const double hf = (double)g.fulcrum_z - (double)det_z;
+        if (std::fabs(sid - hf) < 1e-9 * std::fabs(sid)) return kv_fail(ctx, KV_ERR_GEOMETRY, "fulcrum at the source height");
+        const double mf = sid / (sid - hf);
+        for (int k = 0; k < nz; ++k) {
+            const double hz = -0.5 * nz * (double)g.dz + (k + 0.5) * (double)g.dz - (double)det_z;
+            if (std::fabs(sid - hz) < 1e-9 * std::fabs(sid)) return kv_fail(ctx, KV_ERR_GEOMETRY, "slice %d at the source height", k);
+            const double mz = sid / (sid - hz);
+            for (int i = 0; i < P; ++i)
+                sh[(size_t)k * P + i] = (int32_t)std::lround((double)g.src[3 * i + 1] * (mz - mf) / (double)g.dv);
+        }
+    }
+    return KV_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Library / context
+// ---------------------------------------------------------------------------
+
+extern "C" const char *kv_version(void) { return "kvtomo 0.1.0 (sm_103a)"; }
+
+extern "C" const char *kv_status_string(kv_status s) {
+    switch (s) {
+    case KV_OK: return "ok";
+    case KV_ERR_INVALID_ARG: return "invalid argument";
+    case KV_ERR_GEOMETRY: return "geometry not supported";
+    case KV_ERR_OOM: return "out of memory";
+    case KV_ERR_CUDA: return "CUDA error";
+    case KV_ERR_TIMEOUT: return "device wait timed out";
+    case KV_ERR_NUMERIC: return "numeric error";
+    case KV_ERR_UNSUPPORTED: return "unsupported";
+    case KV_ERR_NO_DEVICE: return "no sm_103 device";
+    }
+    return "unknown status";
+}
+
+extern "C" kv_status kv_ctx_create(int device, kv_ctx **out) {
+    if (out == nullptr) return KV_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return KV_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return KV_ERR_INVALID_ARG;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return KV_ERR_CUDA;
+    if (!(prop.major == 10 && prop.minor == 3)) return KV_ERR_NO_DEVICE;
+    kv_ctx *ctx = new (std::nothrow) kv_ctx;
+    if (ctx == nullptr) return KV_ERR_OOM;
+    ctx->device = device;
+    ctx->sm_count = prop.multiProcessorCount;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->d_red, 8 * sizeof(double)) != cudaSuccess) {
+        if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+        delete ctx;
+        return KV_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->d_red);
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_ctx_set_stream(kv_ctx *ctx, void *stream) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_sync(kv_ctx *ctx) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return KV_OK;
+}
+
+extern "C" const char *kv_ctx_last_error(const kv_ctx *ctx) {
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+
+extern "C" kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *g, kv_family family,
+                                    kv_storage storage, kv_plan **out) {
+    if (ctx == nullptr || g == nullptr || out == nullptr) return KV_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || g->nu <= 0 || g->nv <= 0 || g->n_views <= 0)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "sizes must be positive");
+    if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->du > 0) || !(g->dv > 0))
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "spacings must be positive");
+    if (g->src == nullptr || g->det_origin == nullptr)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "null source / detector array");
+    if ((size_t)g->nx * g->ny >= (1ull << 31) || (size_t)g->nu * g->nv >= (1ull << 31))
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "slice or detector larger than 2^31 elements");
+    if (family != KV_FAMILY_RC && family != KV_FAMILY_EXACT)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad family");
+    if (storage != KV_STORAGE_F32 && storage != KV_STORAGE_BF16 && storage != KV_STORAGE_F16)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad storage");
+    if (family == KV_FAMILY_RC && storage != KV_STORAGE_F32)
+        return kv_fail(ctx, KV_ERR_UNSUPPORTED, "the reference-compatible family is FP32 only");
+    for (int i = 0; i < 3 * g->n_views; ++i)
+        if (!std::isfinite(g->src[i]) || !std::isfinite(g->det_origin[i]))
+            return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite source / detector position");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    kv_plan *plan = new (std::nothrow) kv_plan;
+    if (plan == nullptr) return KV_ERR_OOM;
+    plan->ctx = ctx;
+    plan->g = *g;
+    plan->src.assign(g->src, g->src + 3 * g->n_views);
+    plan->det.assign(g->det_origin, g->det_origin + 3 * g->n_views);
+    plan->g.src = plan->src.data();
+    plan->g.det_origin = plan->det.data();
+    plan->family = family;
+    plan->storage = storage;
+    plan->nvox = (size_t)g->nx * g->ny * g->nz;
+    plan->nproj = (size_t)g->nu * g->nv * g->n_views;
+    kv_status s = KV_OK;
+    if (family == KV_FAMILY_EXACT) {
+        s = exact_build_tables(plan, plan->src.data(), plan->det.data(), g->n_views, &plan->ex);
+    } else {
+        size_t bytes = 3 * sizeof(float) * g->n_views;
+        if (cudaMalloc((void **)&plan->d_src, bytes) != cudaSuccess ||
+            cudaMalloc((void **)&plan->d_org, bytes) != cudaSuccess) {
+            s = kv_fail(ctx, KV_ERR_OOM, "plan tables");
+        } else {
+            cudaMemcpy(plan->d_src, plan->src.data(), bytes, cudaMemcpyHostToDevice);
+            cudaMemcpy(plan->d_org, plan->det.data(), bytes, cudaMemcpyHostToDevice);
+        }
+    }
+    if (s != KV_OK) {
+        kv_plan_destroy(plan);
+        return s;
+    }
+    *out = plan;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_destroy(kv_plan *plan) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    cudaSetDevice(plan->ctx->device);
+    cudaStreamSynchronize(plan->ctx->stream);
+    exact_free_tables(&plan->ex);
+    cudaFree(plan->d_src);
+    cudaFree(plan->d_org);
+    cudaFree(plan->d_vol);
+    cudaFree(plan->d_proj);
+    cudaFree(plan->d_ratio);
+    cudaFree(plan->d_vol32);
+    cudaFree(plan->d_proj32);
+    cudaFree(plan->d_sens);
+    cudaFree(plan->d_shift);
+    delete plan;
+    return KV_OK;
+}
+
+extern "C" size_t kv_plan_volume_elems(const kv_plan *plan) { return plan ? plan->nvox : 0; }
+extern "C" size_t kv_plan_proj_elems(const kv_plan *plan) { return plan ? plan->nproj : 0; }
+
+// ---------------------------------------------------------------------------
+// Operators
+// ---------------------------------------------------------------------------
+
+extern "C" kv_status kv_forward(kv_plan *plan, const float *volume, float *proj, kv_mem mem) {
+    KV_TRY(check_common(plan, volume, proj, mem));
+    float *vd, *pd;
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &vd));
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, false, &pd));
+    if (plan->family == KV_FAMILY_RC) {
+        KV_TRY(rc_forward_launch(plan, plan->d_src, plan->d_org, plan->g.n_views, RC_PLAIN, vd, nullptr, pd, 1.f));
+    } else if (plan->storage == KV_STORAGE_F32) {
+        KV_TRY(exact_forward_launch(plan, plan->ex, plan->g.n_views, FWD_PLAIN, FwdArgs{vd, nullptr, pd, nullptr, 1.f}));
+    } else {
+        const size_t es = kv_storage_bytes(plan->storage);
+        KV_TRY(ensure(plan->ctx, &plan->d_vol, plan->nvox * es));
+        KV_TRY(ensure(plan->ctx, &plan->d_ratio, plan->nproj * es));
+        KV_TRY(convert_launch(plan->ctx, vd, plan->d_vol, plan->nvox, plan->storage));
+        KV_TRY(exact_forward_launch(plan, plan->ex, plan->g.n_views, FWD_PLAIN,
+                                    FwdArgs{plan->d_vol, nullptr, plan->d_ratio, nullptr, 1.f}));
+        KV_TRY(convert_back_launch(plan->ctx, plan->d_ratio, pd, plan->nproj, plan->storage));
+    }
+    return stage_out(plan, proj, mem, pd, plan->nproj);
+}
+
+extern "C" kv_status kv_forward_single(kv_plan *plan, const float *volume, const float src[3],
+                                       const float det_origin[3], float *proj, kv_mem mem) {
+    KV_TRY(check_common(plan, volume, proj, mem));
+    if (src == nullptr || det_origin == nullptr) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "null position");
+    const size_t nout = (size_t)plan->g.nu * plan->g.nv;
+    float *vd, *pd;
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &vd));
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, false, &pd));
+    if (plan->family == KV_FAMILY_RC) {
+        float *d6 = nullptr;
+        KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&d6, 6 * sizeof(float), plan->ctx->stream));
+        float h6[6] = {src[0], src[1], src[2], det_origin[0], det_origin[1], det_origin[2]};
+        KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(d6, h6, sizeof h6, cudaMemcpyHostToDevice, plan->ctx->stream));
+        kv_status s = rc_forward_launch(plan, d6, d6 + 3, 1, RC_PLAIN, vd, nullptr, pd, 1.f);
+        cudaFreeAsync(d6, plan->ctx->stream);
+        KV_TRY(s);
+    } else {
+        if (plan->storage != KV_STORAGE_F32) return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "single-view forward is FP32 only");
+        ExactTables t;
+        KV_TRY(exact_build_tables(plan, src, det_origin, 1, &t));
+        kv_status s = exact_forward_launch(plan, t, 1, FWD_PLAIN, FwdArgs{vd, nullptr, pd, nullptr, 1.f});
+        cudaStreamSynchronize(plan->ctx->stream);
+        exact_free_tables(&t);
+        KV_TRY(s);
+    }
+    return stage_out(plan, proj, mem, pd, nout);
+}
+
+extern "C" kv_status kv_back(kv_plan *plan, const float *proj, float *volume, kv_mem mem) {
+    KV_TRY(check_common(plan, proj, volume, mem));
+    float *pd, *vd;
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, false, &vd));
+    if (plan->family == KV_FAMILY_RC) {
+        KV_TRY(rc_back_launch(plan, RC_PLAIN, pd, vd));
+    } else {
+        const size_t es = kv_storage_bytes(plan->storage);
+        KV_TRY(ensure(plan->ctx, &plan->d_ratio, plan->nproj * es));
+        KV_TRY(exact_prescale_launch(plan, pd, plan->d_ratio));
+        if (plan->storage == KV_STORAGE_F32) {
+            KV_TRY(exact_back_launch(plan, BACK_PLAIN, BackArgs{plan->d_ratio, vd, nullptr, 1.f}));
+        } else {
+            KV_TRY(ensure(plan->ctx, &plan->d_vol, plan->nvox * es));
+            KV_TRY(exact_back_launch(plan, BACK_PLAIN, BackArgs{plan->d_ratio, plan->d_vol, nullptr, 1.f}));
+            KV_TRY(convert_back_launch(plan->ctx, plan->d_vol, vd, plan->nvox, plan->storage));
+        }
+    }
+    return stage_out(plan, volume, mem, vd, plan->nvox);
+}
+
+extern "C" kv_status kv_sensitivity(kv_plan *plan, double *sens, kv_mem mem) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (sens == nullptr) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "null buffer");
+    if (plan->family != KV_FAMILY_EXACT)
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "the sensitivity image is defined for the EXACT family");
+    KV_CHECK_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+    KV_TRY(ensure_sens(plan));
+    KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(sens, plan->d_sens, plan->nvox * sizeof(double),
+                                             mem == KV_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                                             plan->ctx->stream));
+    if (mem == KV_MEM_HOST) KV_CHECK_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
+    return KV_OK;
+}
+
+extern "C" kv_status kv_shift_and_add(kv_plan *plan, const float *proj, float *slices, kv_mem mem) {
+    KV_TRY(check_common(plan, proj, slices, mem));
+    std::vector<int32_t> sh((size_t)plan->g.nz * plan->g.n_views);
+    KV_TRY(saa_shifts(plan->ctx, plan->g, plan->family, sh.data()));
+    const size_t nout = (size_t)plan->g.nz * plan->g.nv * plan->g.nu;
+    KV_TRY(ensure(plan->ctx, &plan->d_shift, sh.size() * sizeof(int32_t)));
+    KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(plan->d_shift, sh.data(), sh.size() * sizeof(int32_t),
+                                             cudaMemcpyHostToDevice, plan->ctx->stream));
+    float *pd, *od = nullptr;
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
+    if (mem == KV_MEM_DEVICE) od = slices;
+    else KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&od, nout * sizeof(float), plan->ctx->stream));
+    kv_status s = saa_launch(plan, plan->d_shift, pd, od);
+    if (s == KV_OK && mem == KV_MEM_HOST) s = stage_out(plan, slices, mem, od, nout);
+    if (mem == KV_MEM_HOST) cudaFreeAsync(od, plan->ctx->stream);
+    return s;
+}
+
+extern "C" kv_status kv_shift_and_add_shifts(const kv_geometry *geom, kv_family family, int32_t *shifts) {
+    if (geom == nullptr || shifts == nullptr || geom->src == nullptr || geom->det_origin == nullptr)
+        return KV_ERR_INVALID_ARG;
+    if (family != KV_FAMILY_RC && family != KV_FAMILY_EXACT) return KV_ERR_INVALID_ARG;
+    return saa_shifts(nullptr, *geom, family, shifts);
+}
+
+extern "C" kv_status kv_phantom_ellipsoids(kv_ctx *ctx, int32_t nx, int32_t ny, int32_t nz, float dx,
+                                           float dy, float dz, const float *params, int32_t n,
+                                           float *volume, kv_mem mem) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (params == nullptr || volume == nullptr || n < 0 || nx <= 0 || ny <= 0 || nz <= 0)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad phantom arguments");
+    if (mem != KV_MEM_HOST && mem != KV_MEM_DEVICE) return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad kv_mem");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t nvox = (size_t)nx * ny * nz;
+    float *dp = nullptr, *dv = nullptr;
+    KV_CHECK_CUDA(ctx, cudaMallocAsync((void **)&dp, (size_t)16 * (n > 0 ? n : 1) * sizeof(float), ctx->stream));
+    if (n > 0) {
+        cudaMemcpyKind kind = mem == KV_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(dp, params, (size_t)16 * n * sizeof(float), kind, ctx->stream));
+    }
+    if (mem == KV_MEM_DEVICE) dv = volume;
+    else KV_CHECK_CUDA(ctx, cudaMallocAsync((void **)&dv, nvox * sizeof(float), ctx->stream));
+    kv_status s = phantom_launch(ctx, nx, ny, nz, dx, dy, dz, dp, n, dv);
+    if (s == KV_OK && mem == KV_MEM_HOST) {
+        cudaError_t e = cudaMemcpyAsync(volume, dv, nvox * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) s = kv_fail(ctx, KV_ERR_CUDA, "phantom copy-out: %s", cudaGetErrorString(e));
+    }
+    cudaFreeAsync(dp, ctx->stream);
+    if (mem == KV_MEM_HOST) cudaFreeAsync(dv, ctx->stream);
+    return s;
+}
+
+extern "C" kv_status kv_uniform_volume(kv_plan *plan, float *volume, kv_mem mem) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (volume == nullptr) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "null buffer");
+    if (mem == KV_MEM_HOST) {
+        for (size_t i = 0; i < plan->nvox; ++i) volume[i] = 1.f;
+        return KV_OK;
+    }
+    KV_CHECK_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+    return fill_launch(plan->ctx, volume, plan->nvox, 1.f);
+}
+
+// ---------------------------------------------------------------------------
+// Iterative drivers
+// ---------------------------------------------------------------------------
+
+kv_status rc_residual_launch(kv_plan *plan, const float *q, const float *p, double *red);
+kv_status rc_ratio_launch(kv_plan *plan, int mode, const float *p, float *q, float relax);
+
+namespace {
+
+// MLEM (mlem = true) or SART/ART (mlem = false) on device buffers: p, x are
+// float32 (RC or F32 storage) or storage-typed (EXACT mixed precision).
+kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax, bool mlem,
+                  kv_iter_cb cb, void *user) {
+    kv_ctx *ctx = plan->ctx;
+    const size_t es = kv_storage_bytes(plan->storage);
+    KV_TRY(ensure(ctx, &plan->d_ratio, plan->nproj * es));
+    if (plan->family == KV_FAMILY_EXACT) KV_TRY(ensure_sens(plan));
+    for (int it = 0; it < iters; ++it) {
+        if (plan->family == KV_FAMILY_EXACT) {
+            FwdArgs fa{x, p, plan->d_ratio, cb ? ctx->d_red : nullptr, relax};
+            KV_TRY(exact_forward_launch(plan, plan->ex, plan->g.n_views, mlem ? FWD_MLEM : FWD_SART, fa));
+        } else if (cb) {
+            KV_TRY(rc_forward_launch(plan, plan->d_src, plan->d_org, plan->g.n_views, RC_PLAIN, (const float *)x,
+                                     nullptr, (float *)plan->d_ratio, relax));
+            KV_TRY(rc_residual_launch(plan, (const float *)plan->d_ratio, (const float *)p, ctx->d_red));
+        } else {
+            KV_TRY(rc_forward_launch(plan, plan->d_src, plan->d_org, plan->g.n_views, mlem ? RC_MLEM : RC_ART,
+                                     (const float *)x, (const float *)p, (float *)plan->d_ratio, relax));
+        }
+        if (cb) {
+            double res = 0.0, ll = 0.0;
+            KV_TRY(residual_from_red(ctx, &res, &ll));
+            if (cb(it, res, ll, user) != 0) return KV_OK;
+            if (plan->family == KV_FAMILY_RC)
+                KV_TRY(rc_ratio_launch(plan, mlem ? RC_MLEM : RC_ART, (const float *)p, (float *)plan->d_ratio, relax));
+        }
+        if (plan->family == KV_FAMILY_EXACT) {
+            BackArgs ba{plan->d_ratio, x, plan->d_sens, relax};
+            KV_TRY(exact_back_launch(plan, mlem ? BACK_MLEM : BACK_SART, ba));
+        } else {
+            KV_TRY(rc_back_launch(plan, mlem ? RC_MLEM : RC_ART, (const float *)plan->d_ratio, (float *)x));
+        }
+    }
+    return KV_OK;
+}
+
+kv_status driver(kv_plan *plan, const float *proj, float *volume, int iters, float relax, kv_mem mem,
+                 kv_iter_cb cb, void *user, bool mlem) {
+    KV_TRY(check_common(plan, proj, volume, mem));
+    if (iters < 0) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "negative iteration count");
+    if (!std::isfinite(relax)) return kv_fail(plan->ctx, KV_ERR_NUMERIC, "non-finite relaxation");
+    float *pd, *xd;
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &xd));
+    if (plan->storage == KV_STORAGE_F32) {
+        KV_TRY(iterate(plan, pd, xd, iters, relax, mlem, cb, user));
+    } else {
+        const size_t es = kv_storage_bytes(plan->storage);
+        KV_TRY(ensure(plan->ctx, &plan->d_vol, plan->nvox * es));
+        KV_TRY(ensure(plan->ctx, &plan->d_proj, plan->nproj * es));
+        KV_TRY(convert_launch(plan->ctx, pd, plan->d_proj, plan->nproj, plan->storage));
+        KV_TRY(convert_launch(plan->ctx, xd, plan->d_vol, plan->nvox, plan->storage));
+        KV_TRY(iterate(plan, plan->d_proj, plan->d_vol, iters, relax, mlem, cb, user));
+        KV_TRY(convert_back_launch(plan->ctx, plan->d_vol, xd, plan->nvox, plan->storage));
+    }
+    return stage_out(plan, volume, mem, xd, plan->nvox);
+}
+
+}  // namespace
+
+extern "C" kv_status kv_mlem(kv_plan *plan, const float *proj, float *volume, int iters, float relax,
+                             kv_mem mem, kv_iter_cb cb, void *user) {
+    return driver(plan, proj, volume, iters, relax, mem, cb, user, true);
+}
+
+extern "C" kv_status kv_sart(kv_plan *plan, const float *proj, float *volume, int iters, float relax,
+                             kv_mem mem, kv_iter_cb cb, void *user) {
+    return driver(plan, proj, volume, iters, relax, mem, cb, user, false);
+}
+
+extern "C" kv_status kv_residual(kv_plan *plan, const float *proj, const float *volume, kv_mem mem,
+                                 double *rel_residual, double *loglik) {
+    KV_TRY(check_common(plan, proj, volume, mem));
+    float *pd, *xd;
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &xd));
+    if (plan->family == KV_FAMILY_EXACT) {
+        const void *pv = pd, *xv = xd;
+        if (plan->storage != KV_STORAGE_F32) {
+            const size_t es = kv_storage_bytes(plan->storage);
+            KV_TRY(ensure(plan->ctx, &plan->d_vol, plan->nvox * es));
+            KV_TRY(ensure(plan->ctx, &plan->d_proj, plan->nproj * es));
+            KV_TRY(convert_launch(plan->ctx, pd, plan->d_proj, plan->nproj, plan->storage));
+            KV_TRY(convert_launch(plan->ctx, xd, plan->d_vol, plan->nvox, plan->storage));
+            pv = plan->d_proj;
+            xv = plan->d_vol;
+        }
+        FwdArgs fa{xv, pv, nullptr, plan->ctx->d_red, 1.f};
+        KV_TRY(exact_forward_launch(plan, plan->ex, plan->g.n_views, FWD_RESID, fa));
+    } else {
+        KV_TRY(ensure(plan->ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
+        KV_TRY(rc_forward_launch(plan, plan->d_src, plan->d_org, plan->g.n_views, RC_PLAIN, xd, nullptr,
+                                 (float *)plan->d_ratio, 1.f));
+        KV_TRY(rc_residual_launch(plan, (const float *)plan->d_ratio, pd, plan->ctx->d_red));
+    }
+    return residual_from_red(plan->ctx, rel_residual, loglik);
+}

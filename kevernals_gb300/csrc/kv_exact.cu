@@ -1,0 +1,509 @@
+// kv_exact.cu -- EXACT family: Siddon line-integral projector A and its exact
+// transpose A^T for the linear-sweep tomosynthesis geometry, on sm_103a.
+//
+// Geometry of a ray.  The detector plane is horizontal, below the volume, and
+// every source is above it.  The x coordinate of the ray through detector
+// pixel (u,v) at height z depends only on u (and the view), its y coordinate
+// only on v.  Every ray crosses every z-plane, so the volume is traversed one
+// z-slice at a time with a slice-local parameter t in [0,1] (t = 0 on the
+// slice's top plane, t = 1 on its bottom plane).  The length of the ray inside
+// voxel (i,j,k) is
+//     Ls(u,v) * [min(1, tx_hi(u,i,k), ty_hi(v,j,k)) - max(0, tx_lo, ty_lo)]+
+// where [tx_lo, tx_hi] is the t-interval in which ray column u lies in the
+// x-slab of column i inside slice k (likewise for y) and Ls = |ray| * dz / H
+// the length of the ray within one slice.
+//
+// The forward kernel walks each ray through its voxels (incremental Siddon:
+// R. L. Siddon, Med. Phys. 12(2) 1985; F. Jacobs et al. 1998) and the
+// backprojector gathers, for each voxel, the rays crossing it.  Both evaluate
+// the plane-crossing parameters with the same float expression
+// (cross_t) from the same per-view tables, so every weight the backprojector
+// uses is bit-identical to the one the forward projector uses: A^T is the
+// exact transpose of A up to the order of the sums.
+#include "kv_internal.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace {
+
+struct ExGeom {
+    int nx, ny, nz, nu, nv, n_views;
+};
+
+__device__ __forceinline__ float cross_t(int rel_plane, float ft, float ix) {
+    return __fmul_rn(__fsub_rn((float)rel_plane, ft), ix);
+}
+
+// Ls = sqrt(ax^2 + ay^2 + H^2) * dz / H : length of the ray inside one slice.
+__device__ __forceinline__ float ray_factor(float ax, float ay, float4 vi) {
+    return __fmul_rn(__fsqrt_rn(__fadd_rn(__fmaf_rn(ax, ax, __fmul_rn(ay, ay)), vi.x)), vi.y);
+}
+
+// Range [k0, k1] of slices in which the ray may be inside the volume laterally.
+__device__ __forceinline__ void lateral_slices(float pos0, float slope, int n, int nz, float &klo,
+                                               float &khi) {
+    // pos(k) = pos0 + slope * k must stay in [0, n]
+    if (fabsf(slope) < 1e-30f) {
+        if (pos0 < 0.f || pos0 > (float)n) { klo = 1.f; khi = 0.f; }
+        else { klo = 0.f; khi = (float)nz; }
+        return;
+    }
+    float a = (0.f - pos0) / slope, b = ((float)n - pos0) / slope;
+    klo = fminf(a, b);
+    khi = fmaxf(a, b);
+}
+
+template <typename VolT, typename ProjT, int MODE>
+__global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T, FwdArgs a,
+                                                        double *partials) {
+    const int u = blockIdx.x * 32 + threadIdx.x;
+    const int v = blockIdx.y * blockDim.y + threadIdx.y;
+    const int p = blockIdx.z;
+    const bool live = (u < G.nu) && (v < G.nv);
+    float acc = 0.f, wsum = 0.f, q = 0.f, pm = 0.f;
+    size_t ray = 0;
+    if (live) {
+        const float4 X = T.xt[(size_t)p * G.nu + u];
+        const int ib = T.xi[(size_t)p * G.nu + u];
+        const float4 Y = T.yt[(size_t)p * G.nv + v];
+        const int jb = T.yi[(size_t)p * G.nv + v];
+        const float4 VI = T.vinfo[p];
+        const float *hr = T.hr + (size_t)p * (G.nz + 1);
+        const int mvx = X.z > 0.f ? 1 : -1, mvy = Y.z > 0.f ? 1 : -1;
+        const int ex = mvx > 0 ? 1 : 0, ey = mvy > 0 ? 1 : 0;
+
+        // lateral clipping to the slices the ray can reach inside the volume
+        const float hr0 = hr[0], dh = VI.y;
+        float kxl, kxh, kyl, kyh;
+        lateral_slices((float)ib + fmaf(X.y, hr0, X.x), X.y * dh, G.nx, G.nz, kxl, kxh);
+        lateral_slices((float)jb + fmaf(Y.y, hr0, Y.x), Y.y * dh, G.ny, G.nz, kyl, kyh);
+        const float klo = fmaxf(kxl, kyl), khi = fminf(kxh, kyh);
+        int k0 = 0, k1 = -1;
+        if (klo <= khi) {
+            k0 = max(0, (int)floorf(klo) - 1);
+            k1 = min(G.nz - 1, (int)ceilf(khi) + 1);
+        }
+        const VolT *vol = static_cast<const VolT *>(a.vol);
+        const size_t plane = (size_t)G.nx * G.ny;
+        for (int k = k1; k >= k0; --k) {
+            const float htop = hr[k + 1];
+            const float ftx = __fmaf_rn(X.y, htop, X.x);
+            const float fty = __fmaf_rn(Y.y, htop, Y.x);
+            int i = mvx > 0 ? (int)floorf(ftx) : (int)ceilf(ftx) - 1;
+            int j = mvy > 0 ? (int)floorf(fty) : (int)ceilf(fty) - 1;
+            float tx = cross_t(i + ex, ftx, X.z);
+            float ty = cross_t(j + ey, fty, Y.z);
+            float t = 0.f;
+            const VolT *slice = vol + (size_t)k * plane;
+            while (true) {
+                const float te = fminf(fminf(tx, ty), 1.0f);
+                const int ai = ib + i, aj = jb + j;
+                if ((unsigned)ai < (unsigned)G.nx && (unsigned)aj < (unsigned)G.ny) {
+                    const float w = __fsub_rn(te, t);
+                    acc = fmaf(w, Store<VolT>::ld(slice + (size_t)aj * G.nx + ai), acc);
+                    if (MODE == FWD_SART) wsum += w;
+                }
+                if (te >= 1.0f) break;
+                if (tx <= ty) {
+                    i += mvx;
+                    tx = cross_t(i + ex, ftx, X.z);
+                } else {
+                    j += mvy;
+                    ty = cross_t(j + ey, fty, Y.z);
+                }
+                t = te;
+            }
+        }
+        const float ls = ray_factor(X.w, Y.w, VI);
+        q = acc * ls;
+        ray = ((size_t)p * G.nv + v) * G.nu + u;
+        ProjT *out = static_cast<ProjT *>(a.out);
+        if (MODE != FWD_PLAIN) pm = Store<ProjT>::ld(static_cast<const ProjT *>(a.meas) + ray);
+        if (MODE == FWD_PLAIN) {
+            Store<ProjT>::st(out + ray, q);
+        } else if (MODE == FWD_MLEM) {
+            const float r = q > 0.f ? a.relax * pm / q : 0.f;
+            Store<ProjT>::st(out + ray, r * ls);
+        } else if (MODE == FWD_SART) {
+            const float rows = wsum * ls;
+            const float r = rows > 0.f ? (pm - q) / rows : 0.f;
+            Store<ProjT>::st(out + ray, r * ls);
+        }
+    }
+    if (partials != nullptr) {
+        // FP64 block reduction of (q - p)^2, p^2 and p log q - q
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+        if (live) {
+            const double dq = (double)q - (double)pm;
+            d0 = dq * dq;
+            d1 = (double)pm * (double)pm;
+            d2 = (q > 0.f ? (double)pm * (double)logf(q) : 0.0) - (double)q;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+            d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+            d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        }
+        __shared__ double red[3][32];
+        const int warp = threadIdx.y, nwarps = blockDim.y;
+        if (threadIdx.x == 0) { red[0][warp] = d0; red[1][warp] = d1; red[2][warp] = d2; }
+        __syncthreads();
+        if (warp == 0) {
+            d0 = threadIdx.x < nwarps ? red[0][threadIdx.x] : 0.0;
+            d1 = threadIdx.x < nwarps ? red[1][threadIdx.x] : 0.0;
+            d2 = threadIdx.x < nwarps ? red[2][threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+                d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+                d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+            }
+            if (threadIdx.x == 0) {
+                const size_t b = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+                partials[3 * b + 0] = d0;
+                partials[3 * b + 1] = d1;
+                partials[3 * b + 2] = d2;
+            }
+        }
+    }
+}
+
+// Sums the per-block partials into out[0..2] (single block).
+__global__ void reduce_partials_kernel(const double *partials, size_t nblocks, double *out) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (size_t b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        s0 += partials[3 * b];
+        s1 += partials[3 * b + 1];
+        s2 += partials[3 * b + 2];
+    }
+    __shared__ double sh[3][1024];
+    sh[0][threadIdx.x] = s0;
+    sh[1][threadIdx.x] = s1;
+    sh[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0][0];
+        out[1] = sh[1][0];
+        out[2] = sh[2][0];
+    }
+}
+
+// y'(u,v) = y(u,v) * Ls(u,v)   (y == nullptr: y' = Ls, used for A^T 1)
+template <typename ProjT>
+__global__ void prescale_kernel(ExGeom G, ExactTables T, const float *y, ProjT *yp) {
+    const int u = blockIdx.x * 32 + threadIdx.x;
+    const int v = blockIdx.y * blockDim.y + threadIdx.y;
+    const int p = blockIdx.z;
+    if (u >= G.nu || v >= G.nv) return;
+    const float ls = ray_factor(T.xt[(size_t)p * G.nu + u].w, T.yt[(size_t)p * G.nv + v].w, T.vinfo[p]);
+    const size_t r = ((size_t)p * G.nv + v) * G.nu + u;
+    Store<ProjT>::st(yp + r, y ? y[r] * ls : ls);
+}
+
+// Gather backprojector.  Block = 32 x BY voxels (i fastest) of one slice k;
+// warp w owns row j.  For every view, each warp computes the slice-local
+// y-intervals of its candidate detector rows once into shared memory; each
+// lane then loops over the candidate columns u of its voxel.
+template <typename VolT, typename ProjT, typename AccT, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T, BackArgs a,
+                                                         double *sens_out) {
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int i = blockIdx.x * 32 + lane;
+    const int j = blockIdx.y * blockDim.y + warp;
+    const int k = blockIdx.z;
+    __shared__ float2 ysh[16][32];
+    const bool live_i = i < G.nx;
+    const bool live_j = j < G.ny;   // warp-uniform
+    const ProjT *yp = static_cast<const ProjT *>(a.yp);
+    AccT acc = 0, comp = 0;
+    if (live_j) {
+        for (int p = 0; p < G.n_views; ++p) {
+            const float *hr = T.hr + (size_t)p * (G.nz + 1);
+            const float htop = hr[k + 1];
+            const float4 r0 = T.rng[(size_t)p * (G.nz + 1) + k];
+            const float4 r1 = T.rng[(size_t)p * (G.nz + 1) + k + 1];
+            // candidate detector rows of voxel row j (warp-uniform)
+            const float vlo = fminf(((float)j - r0.z) * r0.w, ((float)j - r1.z) * r1.w);
+            const float vhi = fmaxf(((float)(j + 1) - r0.z) * r0.w, ((float)(j + 1) - r1.z) * r1.w);
+            const int v0 = max(0, (int)ceilf(fminf(vlo, vhi) - 0.01f));
+            const int v1 = min(G.nv - 1, (int)floorf(fmaxf(vlo, vhi) + 0.01f));
+            // candidate detector columns of voxel column i (per lane)
+            const float ulo = fminf(((float)i - r0.x) * r0.y, ((float)i - r1.x) * r1.y);
+            const float uhi = fmaxf(((float)(i + 1) - r0.x) * r0.y, ((float)(i + 1) - r1.x) * r1.y);
+            int u0 = max(0, (int)ceilf(fminf(ulo, uhi) - 0.01f));
+            int u1 = min(G.nu - 1, (int)floorf(fmaxf(ulo, uhi) + 0.01f));
+            if (!live_i) u1 = u0 - 1;
+            for (int vb = v0; vb <= v1; vb += 32) {
+                const int vv = vb + lane;
+                if (vv <= v1) {
+                    const float4 Y = T.yt[(size_t)p * G.nv + vv];
+                    const int jb = T.yi[(size_t)p * G.nv + vv];
+                    const float fty = __fmaf_rn(Y.y, htop, Y.x);
+                    const float ta = cross_t(j - jb, fty, Y.z), tb = cross_t(j + 1 - jb, fty, Y.z);
+                    ysh[warp][lane] = make_float2(fmaxf(0.f, fminf(ta, tb)), fminf(1.f, fmaxf(ta, tb)));
+                }
+                __syncwarp();
+                const int nvc = min(32, v1 - vb + 1);
+                for (int u = u0; u <= u1; ++u) {
+                    const float4 X = T.xt[(size_t)p * G.nu + u];
+                    const int ib = T.xi[(size_t)p * G.nu + u];
+                    const float ftx = __fmaf_rn(X.y, htop, X.x);
+                    const float ta = cross_t(i - ib, ftx, X.z), tb = cross_t(i + 1 - ib, ftx, X.z);
+                    const float lox = fmaxf(0.f, fminf(ta, tb)), hix = fminf(1.f, fmaxf(ta, tb));
+                    if (!(hix > lox)) continue;
+                    const ProjT *col = yp + ((size_t)p * G.nv + vb) * G.nu + u;
+                    for (int c = 0; c < nvc; ++c) {
+                        const float2 yi = ysh[warp][c];
+                        const float w = __fsub_rn(fminf(hix, yi.y), fmaxf(lox, yi.x));
+                        if (w > 0.f) {
+                            const AccT term = (AccT)w * (AccT)Store<ProjT>::ld(col + (size_t)c * G.nu);
+                            if (KAHAN) {  // compensated (Kahan) summation
+                                const AccT y_ = term - comp;
+                                const AccT t_ = acc + y_;
+                                comp = (t_ - acc) - y_;
+                                acc = t_;
+                            } else {
+                                acc += term;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (!live_i || !live_j) return;
+    const size_t idx = ((size_t)k * G.ny + j) * G.nx + i;
+    if (sens_out != nullptr) {
+        sens_out[idx] = (double)acc;
+        return;
+    }
+    VolT *vol = static_cast<VolT *>(a.vol);
+    const float b = (float)acc;
+    if (MODE == BACK_PLAIN) {
+        Store<VolT>::st(vol + idx, b);
+    } else if (MODE == BACK_MLEM) {
+        const double s = a.sens[idx];
+        if (s > 0.0) Store<VolT>::st(vol + idx, (float)((double)Store<VolT>::ld_rw(vol + idx) * (double)b / s));
+    } else if (MODE == BACK_SART) {
+        const double s = a.sens[idx];
+        if (s > 0.0)
+            Store<VolT>::st(vol + idx, Store<VolT>::ld_rw(vol + idx) + (float)((double)(a.relax * b) / s));
+    }
+}
+
+ExGeom exgeom(const kv_plan *plan, int n_views) {
+    return ExGeom{plan->g.nx, plan->g.ny, plan->g.nz, plan->g.nu, plan->g.nv, n_views};
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Tables (host, double precision)
+// ---------------------------------------------------------------------------
+
+void exact_free_tables(ExactTables *t) {
+    cudaFree(t->xt);
+    cudaFree(t->xi);
+    cudaFree(t->yt);
+    cudaFree(t->yi);
+    cudaFree(t->hr);
+    cudaFree(t->vinfo);
+    cudaFree(t->rng);
+    *t = ExactTables{};
+}
+
+kv_status exact_build_tables(kv_plan *plan, const float *src, const float *det, int P,
+                             ExactTables *out) {
+    const kv_geometry &g = plan->g;
+    kv_ctx *ctx = plan->ctx;
+    const double X0 = -0.5 * g.nx * (double)g.dx, Y0 = -0.5 * g.ny * (double)g.dy;
+    const double Ztop = 0.5 * g.nz * (double)g.dz, Zbot = -Ztop;
+    std::vector<float4> xt((size_t)P * g.nu), yt((size_t)P * g.nv), vinfo(P), rng((size_t)P * (g.nz + 1));
+    std::vector<int> xi((size_t)P * g.nu), yi((size_t)P * g.nv);
+    std::vector<float> hr((size_t)P * (g.nz + 1));
+    for (int p = 0; p < P; ++p) {
+        const double sx = src[3 * p], sy = src[3 * p + 1], sz = src[3 * p + 2];
+        const double ox = det[3 * p], oy = det[3 * p + 1], zd = det[3 * p + 2];
+        if (!(sz > Ztop) || !(zd < Zbot))
+            return kv_fail(ctx, KV_ERR_GEOMETRY,
+                           "view %d: EXACT needs the source above the volume (z=%g > %g) and the "
+                           "detector below it (z=%g < %g)", p, sz, Ztop, zd, Zbot);
+        const double H = sz - zd, dh = g.dz / H, hmid = -zd / H;
+        vinfo[p] = make_float4((float)(H * H), (float)dh, 0.f, 0.f);
+        for (int k = 0; k <= g.nz; ++k) {
+            const double zk = Zbot + k * (double)g.dz;
+            const double h = (zk - zd) / H;
+            hr[(size_t)p * (g.nz + 1) + k] = (float)(zk / H);
+            // x of column u at plane k: Ax + Bx * u (voxel units)
+            const double Bx = g.du * (1.0 - h) / g.dx, By = g.dv * (1.0 - h) / g.dy;
+            const double Ax = ((ox - X0) + (sx - ox) * h + 0.5 * g.du * (1.0 - h)) / g.dx;
+            const double Ay = ((oy - Y0) + (sy - oy) * h + 0.5 * g.dv * (1.0 - h)) / g.dy;
+            rng[(size_t)p * (g.nz + 1) + k] = make_float4((float)Ax, (float)(1.0 / Bx), (float)Ay, (float)(1.0 / By));
+        }
+        auto axis = [&](int n, double o, double d, double s, double B0, double sp, float4 *tab, int *ib,
+                        int &bad) {
+            for (int u = 0; u < n; ++u) {
+                const double pc = o + (u + 0.5) * d;
+                const double c = (pc - B0) / sp;
+                double gr = (s - pc) / sp;
+                if (std::fabs(gr) < 1e-20) gr = gr < 0 ? -1e-20 : 1e-20;
+                if (std::fabs(gr) * dh > 4096.0) bad = 1;  // > 4096 voxel crossings per slice
+                const double cm = c + gr * hmid;
+                const double base = std::floor(cm);
+                tab[u] = make_float4((float)(cm - base), (float)gr, (float)(-1.0 / (gr * dh)), (float)(s - pc));
+                ib[u] = (int)base;
+            }
+        };
+        int bad = 0;
+        axis(g.nu, ox, g.du, sx, X0, g.dx, xt.data() + (size_t)p * g.nu, xi.data() + (size_t)p * g.nu, bad);
+        axis(g.nv, oy, g.dv, sy, Y0, g.dy, yt.data() + (size_t)p * g.nv, yi.data() + (size_t)p * g.nv, bad);
+        if (bad)
+            return kv_fail(ctx, KV_ERR_GEOMETRY,
+                           "view %d: rays cross more than 4096 voxel columns within one slice", p);
+    }
+    ExactTables t;
+    auto up = [&](void **dst, const void *srcp, size_t bytes) -> kv_status {
+        KV_CHECK_CUDA(ctx, cudaMalloc(dst, bytes));
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(*dst, srcp, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        return KV_OK;
+    };
+    kv_status s = KV_OK;
+    if ((s = up((void **)&t.xt, xt.data(), xt.size() * sizeof(float4))) != KV_OK ||
+        (s = up((void **)&t.xi, xi.data(), xi.size() * sizeof(int))) != KV_OK ||
+        (s = up((void **)&t.yt, yt.data(), yt.size() * sizeof(float4))) != KV_OK ||
+        (s = up((void **)&t.yi, yi.data(), yi.size() * sizeof(int))) != KV_OK ||
+        (s = up((void **)&t.hr, hr.data(), hr.size() * sizeof(float))) != KV_OK ||
+        (s = up((void **)&t.vinfo, vinfo.data(), vinfo.size() * sizeof(float4))) != KV_OK ||
+        (s = up((void **)&t.rng, rng.data(), rng.size() * sizeof(float4))) != KV_OK) {
+        exact_free_tables(&t);
+        return s;
+    }
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *out = t;
+    return KV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+namespace {
+template <typename VolT, typename ProjT>
+kv_status fwd_dispatch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode, const FwdArgs &a,
+                       double *partials) {
+    ExGeom G = exgeom(plan, P);
+    dim3 block(32, plan->fwd_by);
+    dim3 grid((G.nu + 31) / 32, (G.nv + plan->fwd_by - 1) / plan->fwd_by, P);
+    cudaStream_t st = plan->ctx->stream;
+    switch (mode) {
+    case FWD_PLAIN: exact_fwd_kernel<VolT, ProjT, FWD_PLAIN><<<grid, block, 0, st>>>(G, t, a, partials); break;
+    case FWD_MLEM: exact_fwd_kernel<VolT, ProjT, FWD_MLEM><<<grid, block, 0, st>>>(G, t, a, partials); break;
+    case FWD_SART: exact_fwd_kernel<VolT, ProjT, FWD_SART><<<grid, block, 0, st>>>(G, t, a, partials); break;
+    case FWD_RESID: exact_fwd_kernel<VolT, ProjT, FWD_RESID><<<grid, block, 0, st>>>(G, t, a, partials); break;
+    }
+    KV_CHECK_LAUNCH(plan->ctx, "exact_fwd_kernel");
+    return KV_OK;
+}
+
+template <typename VolT, typename ProjT>
+kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan) {
+    ExGeom G = exgeom(plan, plan->g.n_views);
+    dim3 block(32, plan->back_by);
+    dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
+    cudaStream_t st = plan->ctx->stream;
+    const ExactTables &t = plan->ex;
+    if (kahan) {
+        switch (mode) {
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, float, BACK_PLAIN, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, float, BACK_MLEM, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, float, BACK_SART, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        }
+    } else {
+        switch (mode) {
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, float, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, float, BACK_MLEM, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, float, BACK_SART, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        }
+    }
+    KV_CHECK_LAUNCH(plan->ctx, "exact_back_kernel");
+    return KV_OK;
+}
+}  // namespace
+
+kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
+                               const FwdArgs &a) {
+    if (plan->fwd_by < 1 || plan->fwd_by > 8) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad forward block");
+    double *partials = nullptr;
+    size_t nblocks = 0;
+    if (a.red != nullptr) {
+        nblocks = (size_t)((plan->g.nu + 31) / 32) * ((plan->g.nv + plan->fwd_by - 1) / plan->fwd_by) * P;
+        KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&partials, nblocks * 3 * sizeof(double), plan->ctx->stream));
+    }
+    kv_status s;
+    switch (plan->storage) {
+    case KV_STORAGE_BF16: s = fwd_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, t, P, mode, a, partials); break;
+    case KV_STORAGE_F16: s = fwd_dispatch<__half, __half>(plan, t, P, mode, a, partials); break;
+    default: s = fwd_dispatch<float, float>(plan, t, P, mode, a, partials); break;
+    }
+    if (partials != nullptr) {
+        if (s == KV_OK) {
+            reduce_partials_kernel<<<1, 1024, 0, plan->ctx->stream>>>(partials, nblocks, a.red);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) s = kv_fail(plan->ctx, KV_ERR_CUDA, "reduce_partials_kernel: %s", cudaGetErrorString(e));
+        }
+        cudaFreeAsync(partials, plan->ctx->stream);
+    }
+    return s;
+}
+
+kv_status exact_back_launch(kv_plan *plan, BackMode mode, const BackArgs &a) {
+    if (plan->back_by < 1 || plan->back_by > 16) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad back block");
+    switch (plan->storage) {
+    case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, true);
+    case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, true);
+    default: return back_dispatch<float, float>(plan, mode, a, false);
+    }
+}
+
+kv_status exact_prescale_launch(kv_plan *plan, const float *y, void *yp) {
+    ExGeom G = exgeom(plan, plan->g.n_views);
+    dim3 block(32, 8), grid((G.nu + 31) / 32, (G.nv + 7) / 8, G.n_views);
+    cudaStream_t st = plan->ctx->stream;
+    switch (plan->storage) {
+    case KV_STORAGE_BF16: prescale_kernel<__nv_bfloat16><<<grid, block, 0, st>>>(G, plan->ex, y, (__nv_bfloat16 *)yp); break;
+    case KV_STORAGE_F16: prescale_kernel<__half><<<grid, block, 0, st>>>(G, plan->ex, y, (__half *)yp); break;
+    default: prescale_kernel<float><<<grid, block, 0, st>>>(G, plan->ex, y, (float *)yp); break;
+    }
+    KV_CHECK_LAUNCH(plan->ctx, "prescale_kernel");
+    return KV_OK;
+}
+
+// A^T 1 with FP64 accumulation.  Uses the plan's ratio workspace (float32
+// view) for the ray factors.
+kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
+    ExGeom G = exgeom(plan, plan->g.n_views);
+    cudaStream_t st = plan->ctx->stream;
+    float *ls = nullptr;
+    KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&ls, plan->nproj * sizeof(float), st));
+    {
+        dim3 block(32, 8), grid((G.nu + 31) / 32, (G.nv + 7) / 8, G.n_views);
+        prescale_kernel<float><<<grid, block, 0, st>>>(G, plan->ex, nullptr, ls);
+    }
+    BackArgs a{ls, nullptr, nullptr, 1.f};
+    dim3 block(32, plan->back_by);
+    dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
+    exact_back_kernel<float, float, double, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(ls, st);
+    if (e != cudaSuccess) return kv_fail(plan->ctx, KV_ERR_CUDA, "sensitivity launch: %s", cudaGetErrorString(e));
+    return KV_OK;
+}

@@ -1,0 +1,216 @@
+// kv_misc.cu -- shift-and-add, phantom rasteriser and elementwise kernels.
+#include "kv_internal.h"
+
+namespace {
+
+// Shift-and-add (recons::ShiftAndAdd, Reconstructors.h:263-379):
+// out[k][v][u] = (1/P) * sum_i in[i][v + t_ki][u], zero outside the ROI.
+// The reference sums the weighted views in double (vtkImageWeightedSum); here
+// the views are summed exactly enough with a float-float (TwoSum) accumulator
+// and the mean is formed in double before rounding to float.
+// Block: 32 columns x 8 rows; each thread loops over a batch of slices so that
+// consecutive slices, whose shifts differ by a few rows, hit the same lines.
+__global__ void __launch_bounds__(256) saa_kernel(int nu, int nv, int nz, int P,
+                                                  const int32_t *__restrict__ shift,
+                                                  const float *__restrict__ proj,
+                                                  float *__restrict__ out, int kb) {
+    extern __shared__ int32_t sh_shift[];
+    const int u = blockIdx.x * 32 + threadIdx.x;
+    const int v = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k0 = blockIdx.z * kb, k1 = min(nz, k0 + kb);
+    for (int t = threadIdx.y * 32 + threadIdx.x; t < (k1 - k0) * P; t += blockDim.x * blockDim.y)
+        sh_shift[t] = shift[(size_t)k0 * P + t];
+    __syncthreads();
+    if (u >= nu || v >= nv) return;
+    const double w = 1.0 / (double)P;
+    for (int k = k0; k < k1; ++k) {
+        float hi = 0.f, lo = 0.f;
+        const int32_t *sk = sh_shift + (size_t)(k - k0) * P;
+        for (int i = 0; i < P; ++i) {
+            const int r = v + sk[i];
+            if (r >= 0 && r < nv) {
+                const float x = __ldg(proj + ((size_t)i * nv + r) * nu + u);
+                const float s = hi + x;                       // TwoSum(hi, x)
+                const float bp = s - hi;
+                const float err = (hi - (s - bp)) + (x - bp);
+                hi = s;
+                lo += err;
+            }
+        }
+        out[((size_t)k * nv + v) * nu + u] = (float)(((double)hi + (double)lo) * w);
+    }
+}
+
+__global__ void fill_kernel(float *p, size_t n, float v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+template <typename T>
+__global__ void to_storage_kernel(const float *in, T *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        Store<T>::st(out + i, in[i]);
+}
+
+template <typename T>
+__global__ void from_storage_kernel(const T *in, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = Store<T>::ld_rw(in + i);
+}
+
+// Ellipsoid phantom sampled at voxel centres.  params: n rows of 16 floats =
+// centre[3], semi-axes[3], M[9] (local = M (q - c)), density.  The float
+// operations and their order are fixed (explicit round-to-nearest
+// intrinsics), so the result is bit-identical on every build.
+__global__ void __launch_bounds__(256) phantom_kernel(int nx, int ny, int nz, float dx, float dy,
+                                                      float dz, const float *__restrict__ params,
+                                                      int n, float *__restrict__ vol) {
+    extern __shared__ float sp[];
+    for (int t = threadIdx.x; t < 16 * n; t += blockDim.x) sp[t] = params[t];
+    __syncthreads();
+    const size_t plane = (size_t)nx * ny, total = plane * nz;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int z = (int)(idx / plane);
+        const size_t rem = idx % plane;
+        const int y = (int)(rem / nx), x = (int)(rem % nx);
+        const float q0 = __fsub_rn(__fmul_rn(__fadd_rn((float)x, 0.5f), dx), __fmul_rn(__fmul_rn(0.5f, (float)nx), dx));
+        const float q1 = __fsub_rn(__fmul_rn(__fadd_rn((float)y, 0.5f), dy), __fmul_rn(__fmul_rn(0.5f, (float)ny), dy));
+        const float q2 = __fsub_rn(__fmul_rn(__fadd_rn((float)z, 0.5f), dz), __fmul_rn(__fmul_rn(0.5f, (float)nz), dz));
+        float val = 0.f;
+        for (int e = 0; e < n; ++e) {
+            const float *p = sp + 16 * e;
+            const float r0 = __fsub_rn(q0, p[0]), r1 = __fsub_rn(q1, p[1]), r2 = __fsub_rn(q2, p[2]);
+            const float l0 = __fadd_rn(__fadd_rn(__fmul_rn(p[6], r0), __fmul_rn(p[7], r1)), __fmul_rn(p[8], r2));
+            const float l1 = __fadd_rn(__fadd_rn(__fmul_rn(p[9], r0), __fmul_rn(p[10], r1)), __fmul_rn(p[11], r2));
+            const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(p[12], r0), __fmul_rn(p[13], r1)), __fmul_rn(p[14], r2));
+            const float t0 = __fdiv_rn(l0, p[3]), t1 = __fdiv_rn(l1, p[4]), t2 = __fdiv_rn(l2, p[5]);
+            const float s = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(t1, t1)), __fmul_rn(t2, t2));
+            if (s <= 1.f) val = __fadd_rn(val, p[15]);
+        }
+        vol[idx] = val;
+    }
+}
+
+// FP64 reduction of {sum (q-p)^2, sum p^2, sum p log q - q} over n rays:
+// grid-stride per-thread sums, one partial triple per block, then a single
+// block adds the partials in a fixed order (deterministic).
+__global__ void __launch_bounds__(256) residual_partials_kernel(const float *__restrict__ q,
+                                                                const float *__restrict__ p, size_t n,
+                                                                double *__restrict__ partials) {
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float qi = q[i], pi = p[i];
+        const double dq = (double)qi - (double)pi;
+        d0 += dq * dq;
+        d1 += (double)pi * (double)pi;
+        d2 += (qi > 0.f ? (double)pi * (double)logf(qi) : 0.0) - (double)qi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+        d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+        d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+    }
+    __shared__ double sh[3][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { sh[0][warp] = d0; sh[1][warp] = d1; sh[2][warp] = d2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { s0 += sh[0][w]; s1 += sh[1][w]; s2 += sh[2][w]; }
+        partials[3 * blockIdx.x] = s0;
+        partials[3 * blockIdx.x + 1] = s1;
+        partials[3 * blockIdx.x + 2] = s2;
+    }
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    __shared__ double sh[3][256];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        s0 += partials[3 * b];
+        s1 += partials[3 * b + 1];
+        s2 += partials[3 * b + 2];
+    }
+    sh[0][threadIdx.x] = s0;
+    sh[1][threadIdx.x] = s1;
+    sh[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = sh[0][0]; out[1] = sh[1][0]; out[2] = sh[2][0]; }
+}
+
+int grid_for(const kv_ctx *ctx, size_t n, int block) {
+    size_t g = (n + block - 1) / block;
+    size_t cap = (size_t)ctx->sm_count * 8;
+    if (cap == 0) cap = 1024;
+    return (int)(g < cap ? (g == 0 ? 1 : g) : cap);
+}
+
+}  // namespace
+
+kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out) {
+    const kv_geometry &g = plan->g;
+    const int kb = 8;
+    dim3 block(32, 8), grid((g.nu + 31) / 32, (g.nv + 7) / 8, (g.nz + kb - 1) / kb);
+    size_t smem = (size_t)kb * g.n_views * sizeof(int32_t);
+    if (smem > 48 * 1024) return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "shift-and-add: too many views");
+    saa_kernel<<<grid, block, smem, plan->ctx->stream>>>(g.nu, g.nv, g.nz, g.n_views, d_shift, proj, out, kb);
+    KV_CHECK_LAUNCH(plan->ctx, "saa_kernel");
+    return KV_OK;
+}
+
+kv_status fill_launch(kv_ctx *ctx, float *p, size_t n, float v) {
+    fill_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(p, n, v);
+    KV_CHECK_LAUNCH(ctx, "fill_kernel");
+    return KV_OK;
+}
+
+kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_storage s) {
+    int gb = grid_for(ctx, n, 256);
+    if (s == KV_STORAGE_BF16) to_storage_kernel<__nv_bfloat16><<<gb, 256, 0, ctx->stream>>>(in, (__nv_bfloat16 *)out, n);
+    else if (s == KV_STORAGE_F16) to_storage_kernel<__half><<<gb, 256, 0, ctx->stream>>>(in, (__half *)out, n);
+    else to_storage_kernel<float><<<gb, 256, 0, ctx->stream>>>(in, (float *)out, n);
+    KV_CHECK_LAUNCH(ctx, "to_storage_kernel");
+    return KV_OK;
+}
+
+kv_status convert_back_launch(kv_ctx *ctx, const void *in, float *out, size_t n, kv_storage s) {
+    int gb = grid_for(ctx, n, 256);
+    if (s == KV_STORAGE_BF16) from_storage_kernel<__nv_bfloat16><<<gb, 256, 0, ctx->stream>>>((const __nv_bfloat16 *)in, out, n);
+    else if (s == KV_STORAGE_F16) from_storage_kernel<__half><<<gb, 256, 0, ctx->stream>>>((const __half *)in, out, n);
+    else from_storage_kernel<float><<<gb, 256, 0, ctx->stream>>>((const float *)in, out, n);
+    KV_CHECK_LAUNCH(ctx, "from_storage_kernel");
+    return KV_OK;
+}
+
+kv_status phantom_launch(kv_ctx *ctx, int nx, int ny, int nz, float dx, float dy, float dz,
+                         const float *d_params, int n, float *vol) {
+    size_t smem = (size_t)16 * n * sizeof(float);
+    if (smem > 200 * 1024) return kv_fail(ctx, KV_ERR_INVALID_ARG, "phantom: too many ellipsoids");
+    if (smem > 48 * 1024)
+        KV_CHECK_CUDA(ctx, cudaFuncSetAttribute(phantom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    size_t total = (size_t)nx * ny * nz;
+    phantom_kernel<<<grid_for(ctx, total, 256), 256, smem, ctx->stream>>>(nx, ny, nz, dx, dy, dz, d_params, n, vol);
+    KV_CHECK_LAUNCH(ctx, "phantom_kernel");
+    return KV_OK;
+}
+
+kv_status residual_reduce_launch(kv_ctx *ctx, const float *q, const float *p, size_t n, double *red) {
+    const int nblocks = ctx->sm_count > 0 ? ctx->sm_count * 4 : 512;
+    double *partials = nullptr;
+    KV_CHECK_CUDA(ctx, cudaMallocAsync((void **)&partials, (size_t)nblocks * 3 * sizeof(double), ctx->stream));
+    residual_partials_kernel<<<nblocks, 256, 0, ctx->stream>>>(q, p, n, partials);
+    sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(partials, nblocks, red);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(partials, ctx->stream);
+    if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "residual reduction: %s", cudaGetErrorString(e));
+    return KV_OK;
+}

@@ -1,0 +1,256 @@
+"""Python host API over the C ABI: contexts and plans.
+
+A Plan holds one geometry, an operator family ("rc": the reference's own
+operators; "exact": Siddon A and its exact transpose) and a storage type.
+Buffers may be numpy arrays (host memory: the library copies in and out) or
+CUDA torch tensors (device memory: used in place, ordered on the current
+torch stream).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import KvError, KvGeometry, lib
+
+try:  # torch is optional: only needed for device-resident buffers
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_cuda_tensor(x):
+    return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
+
+
+class Context:
+    """A device plus a stream (kv_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        s = lib().kv_ctx_create(device, C.byref(h))
+        if s != _lib.KV_OK:
+            raise KvError(s, lib().kv_status_string(s).decode())
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self) -> str:
+        return lib().kv_ctx_last_error(self._h).decode()
+
+    def check(self, status):
+        if status != _lib.KV_OK:
+            raise KvError(status, self.last_error())
+
+    def set_stream(self, stream_handle):
+        self.check(lib().kv_ctx_set_stream(self._h, C.c_void_p(stream_handle or 0)))
+
+    def use_torch_stream(self):
+        if torch is not None and torch.cuda.is_available():
+            self.set_stream(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def sync(self):
+        self.check(lib().kv_sync(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().kv_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_cgeom(g):
+    src = np.ascontiguousarray(g.src, np.float32)
+    det = np.ascontiguousarray(g.det_origin, np.float32)
+    cg = KvGeometry(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, src.shape[0], g.nu, g.nv, g.du, g.dv,
+                    src.ctypes.data_as(C.POINTER(C.c_float)),
+                    det.ctypes.data_as(C.POINTER(C.c_float)), g.fulcrum_z)
+    cg._keep = (src, det)
+    return cg
+
+
+class Plan:
+    """kv_plan: geometry + operator family + storage type."""
+
+    def __init__(self, ctx: Context, geometry, family: str = "exact", storage: str = "f32"):
+        self.ctx = ctx
+        self.geometry = geometry
+        self.family = family
+        self.storage = storage
+        h = C.c_void_p()
+        cg = make_cgeom(geometry)
+        s = lib().kv_plan_create(ctx.handle, C.byref(cg), _lib.FAMILY[family],
+                                 _lib.STORAGE[storage], C.byref(h))
+        ctx.check(s)
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().kv_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- buffer helpers --------------------------------------------------
+    def _buf(self, x, shape, dtype=np.float32, out=False):
+        """Returns (pointer, mem flag, keep-alive)."""
+        if _is_cuda_tensor(x):
+            want = {np.float32: torch.float32, np.float64: torch.float64}[dtype]
+            if x.dtype != want or not x.is_contiguous() or x.numel() != int(np.prod(shape)):
+                raise ValueError(f"device buffer must be contiguous {want} with {np.prod(shape)} elements")
+            self.ctx.use_torch_stream()
+            return C.c_void_p(x.data_ptr()), _lib.MEM_DEVICE, x
+        a = np.asarray(x)
+        if out:
+            if a.dtype != dtype or not a.flags.c_contiguous or a.size != int(np.prod(shape)):
+                raise ValueError("output array has the wrong dtype / size / layout")
+        else:
+            a = np.ascontiguousarray(a, dtype)
+            if a.size != int(np.prod(shape)):
+                raise ValueError(f"expected {int(np.prod(shape))} elements, got {a.size}")
+        return C.c_void_p(a.ctypes.data), _lib.MEM_HOST, a
+
+    def _like(self, x, shape, dtype=np.float32):
+        if _is_cuda_tensor(x):
+            return torch.empty(shape, dtype={np.float32: torch.float32, np.float64: torch.float64}[dtype],
+                               device=x.device)
+        return np.empty(shape, dtype)
+
+    # -- operators -------------------------------------------------------
+    def forward(self, volume, out=None):
+        g = self.geometry
+        out = self._like(volume, g.proj_shape) if out is None else out
+        pv, mv, kv = self._buf(volume, g.volume_shape)
+        po, mo, ko = self._buf(out, g.proj_shape, out=True)
+        if mv != mo:
+            raise ValueError("input and output must both be host or both be device buffers")
+        self.ctx.check(lib().kv_forward(self._h, pv, po, mv))
+        return out
+
+    def forward_single(self, volume, src, det_origin, out=None):
+        g = self.geometry
+        shape = (g.nv, g.nu)
+        out = self._like(volume, shape) if out is None else out
+        pv, mv, kv = self._buf(volume, g.volume_shape)
+        po, mo, ko = self._buf(out, shape, out=True)
+        s = (C.c_float * 3)(*[float(t) for t in src])
+        d = (C.c_float * 3)(*[float(t) for t in det_origin])
+        self.ctx.check(lib().kv_forward_single(self._h, pv, C.cast(s, C.c_void_p),
+                                               C.cast(d, C.c_void_p), po, mv))
+        return out
+
+    def back(self, proj, out=None):
+        g = self.geometry
+        out = self._like(proj, g.volume_shape) if out is None else out
+        pp, mp, kp = self._buf(proj, g.proj_shape)
+        po, mo, ko = self._buf(out, g.volume_shape, out=True)
+        self.ctx.check(lib().kv_back(self._h, pp, po, mp))
+        return out
+
+    def sensitivity(self, out=None, device=False):
+        g = self.geometry
+        if out is None:
+            out = (torch.empty(g.volume_shape, dtype=torch.float64, device=f"cuda:{self.ctx.device}")
+                   if device else np.empty(g.volume_shape, np.float64))
+        po, mo, ko = self._buf(out, g.volume_shape, np.float64, out=True)
+        self.ctx.check(lib().kv_sensitivity(self._h, po, mo))
+        return out
+
+    def shift_and_add(self, proj, out=None):
+        g = self.geometry
+        shape = (g.nz, g.nv, g.nu)
+        out = self._like(proj, shape) if out is None else out
+        pp, mp, kp = self._buf(proj, g.proj_shape)
+        po, mo, ko = self._buf(out, shape, out=True)
+        self.ctx.check(lib().kv_shift_and_add(self._h, pp, po, mp))
+        return out
+
+    def uniform_volume(self, device=False):
+        g = self.geometry
+        out = (torch.empty(g.volume_shape, dtype=torch.float32, device=f"cuda:{self.ctx.device}")
+               if device else np.empty(g.volume_shape, np.float32))
+        po, mo, ko = self._buf(out, g.volume_shape, out=True)
+        self.ctx.check(lib().kv_uniform_volume(self._h, po, mo))
+        return out
+
+    def _iterate(self, fn, proj, volume, iterations, relax, callback):
+        g = self.geometry
+        pp, mp, kp = self._buf(proj, g.proj_shape)
+        if not _is_cuda_tensor(volume):
+            if not (isinstance(volume, np.ndarray) and volume.dtype == np.float32
+                    and volume.flags.c_contiguous):
+                raise ValueError("the iterate must be a C-contiguous float32 array (updated in place)")
+        px, mx, kx = self._buf(volume, g.volume_shape, out=True)
+        if mp != mx:
+            raise ValueError("projections and volume must both be host or both be device buffers")
+        history = []
+
+        def _cb(it, res, ll, user):
+            history.append((it, res, ll))
+            return int(bool(callback(it, res, ll))) if callback else 0
+        cb = _lib.ITER_CB(_cb) if callback is not None else _lib.ITER_CB()
+        self.ctx.check(fn(self._h, pp, px, int(iterations), float(relax), mp, cb, None))
+        return history
+
+    def mlem(self, proj, volume, iterations, relax=1.0, callback=None):
+        """In-place MLEM on `volume`; returns the (iteration, residual, loglik)
+        history when a callback is given."""
+        return self._iterate(lib().kv_mlem, proj, volume, iterations, relax, callback)
+
+    def sart(self, proj, volume, iterations, relax=0.5, callback=None):
+        return self._iterate(lib().kv_sart, proj, volume, iterations, relax, callback)
+
+    def residual(self, proj, volume):
+        g = self.geometry
+        pp, mp, kp = self._buf(proj, g.proj_shape)
+        px, mx, kx = self._buf(volume, g.volume_shape)
+        r, ll = C.c_double(), C.c_double()
+        self.ctx.check(lib().kv_residual(self._h, pp, px, mp, C.byref(r), C.byref(ll)))
+        return r.value, ll.value
+
+
+def shift_and_add_shifts(geometry, family: str = "exact") -> np.ndarray:
+    """Row shifts [nz, n_views] of shift-and-add, computed on the host."""
+    out = np.empty((geometry.nz, geometry.n_views), np.int32)
+    cg = make_cgeom(geometry)
+    s = lib().kv_shift_and_add_shifts(C.byref(cg), _lib.FAMILY[family], C.c_void_p(out.ctypes.data))
+    if s != _lib.KV_OK:
+        raise KvError(s, "shift-and-add geometry rejected")
+    return out
+
+
+def phantom(ctx: Context, geometry, params, device=False):
+    """Rasterises ellipsoid parameters (kevernals_gb300.phantom.ellipsoid_params)."""
+    g = geometry
+    params = np.ascontiguousarray(params, np.float32)
+    if device:
+        out = torch.empty(g.volume_shape, dtype=torch.float32, device=f"cuda:{ctx.device}")
+        ctx.use_torch_stream()
+        prm = torch.from_numpy(params).to(out.device)
+        ctx.check(lib().kv_phantom_ellipsoids(ctx.handle, g.nx, g.ny, g.nz, g.dx, g.dy, g.dz,
+                                              C.c_void_p(prm.data_ptr()), params.shape[0],
+                                              C.c_void_p(out.data_ptr()), _lib.MEM_DEVICE))
+        return out
+    out = np.empty(g.volume_shape, np.float32)
+    ctx.check(lib().kv_phantom_ellipsoids(ctx.handle, g.nx, g.ny, g.nz, g.dx, g.dy, g.dz,
+                                          C.c_void_p(params.ctypes.data), params.shape[0],
+                                          C.c_void_p(out.ctypes.data), _lib.MEM_HOST))
+    return out

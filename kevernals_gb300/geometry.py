@@ -1,0 +1,125 @@
+"""Geometry description of a linear-sweep tomosynthesis acquisition.
+
+Mirrors what the reference's TomoGeometry hands to its projector
+(source/modules/geometry/TomoGeometry.h:34-89 and the flattening in
+source/modules/reconstruction/Projector.cu:917-940): volume size and voxel
+spacing, a volume-centred frame (TomoGeometry.cpp:127,162,330), per-view
+source positions, per-view detector-ROI bottom-left corners on a common
+detector plane, ROI size and pixel spacing, and the fulcrum height used by
+shift-and-add.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Geometry:
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    nu: int
+    nv: int
+    du: float
+    dv: float
+    src: np.ndarray          # [n_views, 3] float32, volume-centred frame
+    det_origin: np.ndarray   # [n_views, 3] float32, bottom-left corner of pixel (0,0)
+    fulcrum_z: float = 0.0   # shift-and-add focal height (see kv_geometry)
+
+    def __post_init__(self):
+        # the C ABI carries spacings as float32: keep exactly those values here
+        for f in ("dx", "dy", "dz", "du", "dv", "fulcrum_z"):
+            setattr(self, f, float(np.float32(getattr(self, f))))
+        self.src = np.ascontiguousarray(self.src, dtype=np.float32).reshape(-1, 3)
+        self.det_origin = np.ascontiguousarray(self.det_origin, dtype=np.float32).reshape(-1, 3)
+        if self.src.shape != self.det_origin.shape:
+            raise ValueError("src and det_origin must both be [n_views, 3]")
+
+    @property
+    def n_views(self) -> int:
+        return int(self.src.shape[0])
+
+    @property
+    def volume_shape(self):
+        """numpy shape of a volume: (nz, ny, nx)."""
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def proj_shape(self):
+        """numpy shape of a projection stack: (n_views, nv, nu)."""
+        return (self.n_views, self.nv, self.nu)
+
+    @property
+    def n_voxels(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    @property
+    def n_rays(self) -> int:
+        return self.n_views * self.nu * self.nv
+
+    def subset_views(self, views) -> "Geometry":
+        views = np.asarray(views)
+        return dataclasses.replace(self, src=self.src[views].copy(),
+                                   det_origin=self.det_origin[views].copy())
+
+
+def linear_sweep(nx, ny, nz, dx, dy, dz, n_views, nu, nv, du, dv, half_angle_deg,
+                 sid=1000.0, sod=850.0, gap=10.0) -> Geometry:
+    """Linear-sweep geometry in the volume-centred frame.
+
+    World frame: detector plane z = 0, centred on x = y = 0; the volume sits
+    laterally centred with its bottom face `gap` mm above the detector.  The
+    tube moves along y at height `sid`; its central ray through the isocentre
+    (height sid - sod above the detector) makes the angle theta_i, equally
+    spaced over [-half_angle, +half_angle], so y_i = sod * tan(theta_i).  All
+    positions are then translated so that the volume centre is the origin.
+    The fulcrum height is the isocentre, in the same frame.
+    """
+    zc = gap + 0.5 * nz * dz                      # volume centre height (world)
+    theta = np.deg2rad(np.linspace(-half_angle_deg, half_angle_deg, n_views)) \
+        if n_views > 1 else np.zeros(1)
+    ys = sod * np.tan(theta)
+    src = np.zeros((n_views, 3), np.float64)
+    src[:, 1] = ys
+    src[:, 2] = sid - zc
+    det = np.zeros((n_views, 3), np.float64)
+    det[:, 0] = -0.5 * nu * du
+    det[:, 1] = -0.5 * nv * dv
+    det[:, 2] = -zc
+    return Geometry(nx, ny, nz, float(dx), float(dy), float(dz), nu, nv, float(du), float(dv),
+                    src.astype(np.float32), det.astype(np.float32),
+                    fulcrum_z=float((sid - sod) - zc))
+
+
+# ---- the workloads of the benchmark configurations -----------------------
+
+def config_small() -> Geometry:
+    """256x256x64 at 0.5x0.5x1.0 mm, 15 views over +-15 deg, 512^2 at 0.4 mm."""
+    return linear_sweep(256, 256, 64, 0.5, 0.5, 1.0, 15, 512, 512, 0.4, 0.4, 15.0)
+
+
+def config_chest() -> Geometry:
+    """Chest-DT size: 1024x1024x128 at 0.4x0.4x2.5 mm, 60 views over +-17.5 deg,
+    2048^2 detector at 0.2 mm."""
+    return linear_sweep(1024, 1024, 128, 0.4, 0.4, 2.5, 60, 2048, 2048, 0.2, 0.2, 17.5)
+
+
+def scaled(g: Geometry, factor: int) -> Geometry:
+    """Same physical acquisition with volume and detector sampled `factor`
+    times coarser (used for quick checks of a large workload)."""
+    return linear_sweep(g.nx // factor, g.ny // factor, g.nz, g.dx * factor, g.dy * factor, g.dz,
+                        g.n_views, g.nu // factor, g.nv // factor, g.du * factor, g.dv * factor,
+                        _half_angle(g))
+
+
+def _half_angle(g: Geometry) -> float:
+    zc = -float(g.det_origin[0, 2])
+    sid = float(g.src[0, 2]) + zc
+    sod = sid - (float(g.fulcrum_z) + zc)
+    return math.degrees(math.atan(abs(float(g.src[:, 1].max())) / sod))

@@ -1,0 +1,41 @@
+"""Builds the CPU oracle (TEST INFRASTRUCTURE).
+
+liboracle.so   kvtomo_oracle.c, gcc -O2 -fopenmp -ffp-contract=off (no fused
+               multiply-add, so the RC restatement is bit-identical to the
+               reference kernels compiled for the host).
+_ref/libkvref.so  the reference's own kernels, compiled from the reference
+               tree by build_ref.sh when that tree is present.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libkvref.so")
+REFERENCE_ROOT = "/root/reference"
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "kvtomo_oracle.c")
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src)):
+        return ORACLE_SO
+    cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           src, "-o", ORACLE_SO, "-lm"]
+    subprocess.run(cmd, check=True)
+    return ORACLE_SO
+
+
+def build_ref(force=False):
+    """Compiles the reference kernels when the reference tree is present."""
+    if not os.path.isdir(REFERENCE_ROOT):
+        return None
+    if not force and os.path.exists(REF_SO):
+        return REF_SO
+    subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

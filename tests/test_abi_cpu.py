@@ -1,0 +1,72 @@
+"""CPU tests of the C-ABI library: it builds, loads, exports every symbol the
+header declares, and its host-only logic works without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from kevernals_gb300 import _lib, build, engine
+from kevernals_gb300.geometry import config_small, linear_sweep
+from oracle import oracle as O
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "kvtomo.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(kv_[a-z0-9_]+)\s*\(", text)) - {"kv_iter_cb"})
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.lib()
+
+
+def test_header_declares_the_api():
+    syms = declared_symbols()
+    for s in ("kv_forward", "kv_back", "kv_mlem", "kv_sart", "kv_shift_and_add", "kv_plan_create"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES), "binding misses a declared symbol"
+
+
+def test_status_strings(lib):
+    assert lib.kv_status_string(0) == b"ok"
+    assert b"sm_103" in lib.kv_status_string(8)
+    assert lib.kv_version().startswith(b"kvtomo")
+
+
+def test_no_device_is_reported_not_fatal(lib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    h = C.c_void_p()
+    assert lib.kv_ctx_create(0, C.byref(h)) == 8   # KV_ERR_NO_DEVICE
+    assert not h.value
+    assert lib.kv_ctx_destroy(None) == 1
+
+
+@pytest.mark.parametrize("family,rule", [("rc", 0), ("exact", 1)])
+def test_shift_rule_matches_oracle(lib, family, rule):
+    for g in (config_small(), linear_sweep(32, 32, 17, 0.4, 0.4, 2.5, 9, 64, 64, 0.3, 0.3, 25.0)):
+        assert np.array_equal(engine.shift_and_add_shifts(g, family), O.saa_shifts(g, rule))
+
+
+def test_shift_rule_rejects_degenerate_geometry(lib):
+    g = linear_sweep(8, 8, 1, 0.5, 0.5, 1.0, 3, 8, 8, 0.5, 0.5, 10.0)   # one slice
+    with pytest.raises(_lib.KvError):
+        engine.shift_and_add_shifts(g, "rc")
+    g = linear_sweep(8, 8, 4, 0.5, 0.5, 1.0, 1, 8, 8, 0.5, 0.5, 10.0)   # one view
+    with pytest.raises(_lib.KvError):
+        engine.shift_and_add_shifts(g, "exact")

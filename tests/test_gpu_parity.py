@@ -1,0 +1,318 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the
+oracle (FP32 restatement of the reference for RC, FP64 Siddon for EXACT) and
+against the golden outputs of the reference kernels."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from kevernals_gb300 import build, engine, phantom as ph
+from kevernals_gb300._lib import KvError
+from kevernals_gb300.geometry import Geometry, config_chest, config_small, linear_sweep, scaled
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+# Tolerances (stated): EXACT FP32 GPU vs FP64 oracle
+EXACT_FWD_REL_L2 = 2e-6
+EXACT_BACK_REL_L2 = 2e-6
+DOT_REL = 1e-6
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    build.build()
+    return engine.Context(0)
+
+
+def golden_cases():
+    z = np.load(os.path.join(GOLDEN, "golden_small.npz"))
+    out = {}
+    for name in ("a", "b", "c"):
+        nx, ny, nz, nu, nv = (int(t) for t in z[f"{name}_dims"])
+        dx, dy, dz, du, dv, fz = (float(t) for t in z[f"{name}_spacing"])
+        g = Geometry(nx, ny, nz, dx, dy, dz, nu, nv, du, dv, z[f"{name}_src"], z[f"{name}_det"], fz)
+        out[name] = (g, {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "_")})
+    return out
+
+
+def small_geoms():
+    return [
+        linear_sweep(40, 36, 12, 0.5, 0.5, 1.0, 5, 48, 44, 0.4, 0.4, 15.0),
+        linear_sweep(33, 29, 7, 0.7, 0.45, 1.3, 4, 37, 41, 0.55, 0.35, 22.0),
+        linear_sweep(64, 64, 16, 0.4, 0.4, 2.5, 9, 96, 96, 0.2, 0.2, 17.5),
+    ]
+
+
+def phantom_for(g, n=8, seed=5):
+    return O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n, seed))
+
+
+# ---------------------------------------------------------------- RC family
+
+@pytest.mark.parametrize("name", ["a", "b", "c"])
+def test_rc_forward_back_bitexact_vs_reference_golden(ctx, name):
+    g, d = golden_cases()[name]
+    plan = engine.Plan(ctx, g, "rc")
+    vol = engine.phantom(ctx, g, d["params"])
+    assert np.array_equal(vol, d["vol"])
+    f = plan.forward(vol)
+    assert np.array_equal(f, d["fwd"]), f"max diff {np.abs(f - d['fwd']).max()}"
+    assert np.array_equal(plan.back(d["fwd"]), d["back"])
+    assert np.array_equal(plan.back(d["y"]), d["back_y"])
+
+
+def test_rc_config1_bitexact_vs_reference_digests(ctx):
+    info = json.load(open(os.path.join(GOLDEN, "golden_config1.json")))
+    g = config_small()
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 40, info["seed"])
+    vol = engine.phantom(ctx, g, params)
+    dg = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    assert dg(vol) == info["phantom_sha256"]
+    plan = engine.Plan(ctx, g, "rc")
+    f = plan.forward(vol)
+    assert dg(f) == info["ref_forward_sha256"]
+    assert dg(plan.back(f)) == info["ref_back_of_forward_sha256"]
+
+
+def test_rc_drivers_match_oracle(ctx):
+    g = small_geoms()[0]
+    truth = phantom_for(g)
+    p = O.rc_forward(g, truth)
+    plan = engine.Plan(ctx, g, "rc")
+    for relax in (1.0, 0.5):
+        x = np.ones(g.volume_shape, np.float32)
+        plan.mlem(p, x, 3, relax)
+        assert np.array_equal(x, O.rc_mlem(g, p, np.ones(g.volume_shape, np.float32), 3, relax))
+        x = np.ones(g.volume_shape, np.float32)
+        plan.sart(p, x, 3, relax)
+        assert np.array_equal(x, O.rc_art(g, p, np.ones(g.volume_shape, np.float32), 3, relax))
+    # the callback path (unfused ratio) gives the same iterate
+    x1 = np.ones(g.volume_shape, np.float32)
+    hist = plan.mlem(p, x1, 3, 0.5, callback=lambda it, r, ll: False)
+    assert len(hist) == 3 and hist[0][1] > hist[-1][1]
+    assert np.array_equal(x1, O.rc_mlem(g, p, np.ones(g.volume_shape, np.float32), 3, 0.5))
+
+
+def test_rc_random_geometries_match_oracle(ctx):
+    rng = np.random.default_rng(11)
+    for g in small_geoms():
+        vol = rng.random(g.volume_shape, dtype=np.float32)
+        plan = engine.Plan(ctx, g, "rc")
+        f = plan.forward(vol)
+        assert np.array_equal(f, O.rc_forward(g, vol))
+        assert np.array_equal(plan.back(f), O.rc_back(g, f))
+
+
+# ------------------------------------------------------------- EXACT family
+
+@pytest.mark.parametrize("gi", [0, 1, 2])
+def test_exact_forward_vs_fp64_oracle(ctx, gi):
+    g = small_geoms()[gi]
+    vol = phantom_for(g)
+    plan = engine.Plan(ctx, g, "exact")
+    f = plan.forward(vol)
+    ref = O.exact_forward(g, vol.astype(np.float64))
+    assert rel_l2(f, ref) < EXACT_FWD_REL_L2
+    rng = np.random.default_rng(gi)
+    x = rng.random(g.volume_shape, dtype=np.float32)
+    assert rel_l2(plan.forward(x), O.exact_forward(g, x.astype(np.float64))) < 1e-5
+
+
+@pytest.mark.parametrize("gi", [0, 1, 2])
+def test_exact_back_vs_fp64_oracle(ctx, gi):
+    g = small_geoms()[gi]
+    rng = np.random.default_rng(gi + 10)
+    y = rng.random(g.proj_shape, dtype=np.float32)
+    plan = engine.Plan(ctx, g, "exact")
+    b = plan.back(y)
+    assert rel_l2(b, O.exact_back(g, y.astype(np.float64))) < EXACT_BACK_REL_L2
+
+
+@pytest.mark.parametrize("gi", [0, 1, 2])
+def test_exact_dot_product(ctx, gi):
+    g = small_geoms()[gi]
+    rng = np.random.default_rng(gi + 20)
+    x = rng.random(g.volume_shape, dtype=np.float32)
+    y = rng.random(g.proj_shape, dtype=np.float32)
+    plan = engine.Plan(ctx, g, "exact")
+    lhs = np.vdot(plan.forward(x).astype(np.float64), y.astype(np.float64))
+    rhs = np.vdot(x.astype(np.float64), plan.back(y).astype(np.float64))
+    assert abs(lhs - rhs) <= DOT_REL * abs(lhs)
+
+
+def test_exact_sensitivity_vs_oracle(ctx):
+    g = small_geoms()[0]
+    plan = engine.Plan(ctx, g, "exact")
+    s = plan.sensitivity()
+    assert rel_l2(s, O.exact_back(g, np.ones(g.proj_shape))) < 1e-6
+
+
+def test_exact_mlem_sart_vs_fp64_oracle(ctx):
+    g = small_geoms()[0]
+    truth = phantom_for(g)
+    p = O.exact_forward(g, truth.astype(np.float64)).astype(np.float32)
+    plan = engine.Plan(ctx, g, "exact")
+    x = np.ones(g.volume_shape, np.float32)
+    hist = plan.mlem(p, x, 5, callback=lambda *a: False)
+    xo = O.exact_mlem(g, p.astype(np.float64), np.ones(g.volume_shape), 5)
+    assert rel_l2(x, xo) < 1e-5
+    assert all(b[1] < a[1] for a, b in zip(hist, hist[1:]))
+    x = np.zeros(g.volume_shape, np.float32)
+    plan.sart(p, x, 5, 0.5)
+    xo = O.exact_sart(g, p.astype(np.float64), np.zeros(g.volume_shape), 5, 0.5)
+    assert rel_l2(x, xo) < 1e-5
+
+
+def test_exact_residual_matches_numpy(ctx):
+    g = small_geoms()[1]
+    truth = phantom_for(g)
+    p = O.exact_forward(g, truth.astype(np.float64)).astype(np.float32)
+    plan = engine.Plan(ctx, g, "exact")
+    x = np.full(g.volume_shape, 0.01, np.float32)
+    r, ll = plan.residual(p, x)
+    q = O.exact_forward(g, x.astype(np.float64))
+    pd = p.astype(np.float64)
+    assert r == pytest.approx(np.linalg.norm(q - pd) / np.linalg.norm(pd), rel=1e-5)
+    llo = np.sum(np.where(q > 0, pd * np.log(np.maximum(q, 1e-300)), 0.0) - q)
+    assert ll == pytest.approx(llo, rel=1e-5)
+
+
+def test_mixed_precision_close_to_fp32(ctx):
+    g = small_geoms()[0]
+    truth = phantom_for(g)
+    p = O.exact_forward(g, truth.astype(np.float64)).astype(np.float32)
+    ref = np.ones(g.volume_shape, np.float32)
+    engine.Plan(ctx, g, "exact").mlem(p, ref, 5)
+    for storage, tol in (("bf16", 2e-2), ("f16", 3e-3)):
+        x = np.ones(g.volume_shape, np.float32)
+        engine.Plan(ctx, g, "exact", storage).mlem(p, x, 5)
+        assert rel_l2(x, ref) < tol, storage
+
+
+# ----------------------------------------------------------- shift-and-add
+
+@pytest.mark.parametrize("family,rule", [("rc", 0), ("exact", 1)])
+def test_shift_and_add_vs_oracle(ctx, family, rule):
+    g = small_geoms()[2]
+    rng = np.random.default_rng(4)
+    p = rng.random(g.proj_shape, dtype=np.float32)
+    out = engine.Plan(ctx, g, family).shift_and_add(p)
+    ref = O.saa(g, p, rule)
+    assert np.abs(out - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+# ---------------------------------------------------------------- edges
+
+def test_device_buffers_match_host(ctx):
+    torch = pytest.importorskip("torch")
+    g = small_geoms()[0]
+    vol = phantom_for(g)
+    for fam in ("rc", "exact"):
+        plan = engine.Plan(ctx, g, fam)
+        fh = plan.forward(vol)
+        fd = plan.forward(torch.from_numpy(vol).cuda())
+        torch.cuda.synchronize()
+        assert np.array_equal(fd.cpu().numpy(), fh)
+        bh = plan.back(fh)
+        bd = plan.back(torch.from_numpy(fh).cuda())
+        torch.cuda.synchronize()
+        assert np.array_equal(bd.cpu().numpy(), bh)
+
+
+def test_rays_missing_the_volume_are_zero(ctx):
+    g = linear_sweep(16, 16, 4, 0.5, 0.5, 1.0, 3, 40, 40, 0.5, 0.5, 10.0)
+    det = g.det_origin.copy()
+    det[:, 0] += 15.0                     # half the detector sees no volume
+    g = Geometry(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, g.nu, g.nv, g.du, g.dv, g.src, det, g.fulcrum_z)
+    vol = np.ones(g.volume_shape, np.float32)
+    for fam in ("rc", "exact"):
+        f = engine.Plan(ctx, g, fam).forward(vol)
+        assert (f[:, :, -5:] == 0).all() and (f > 0).any()
+
+
+def test_tiny_and_single_view_geometries(ctx):
+    for g in (linear_sweep(1, 1, 1, 1.0, 1.0, 1.0, 1, 3, 3, 0.5, 0.5, 0.0),
+              linear_sweep(5, 3, 2, 1.0, 1.0, 1.0, 2, 7, 1, 0.8, 0.8, 5.0)):
+        vol = np.arange(1, g.n_voxels + 1, dtype=np.float32).reshape(g.volume_shape)
+        pe = engine.Plan(ctx, g, "exact")
+        assert rel_l2(pe.forward(vol), O.exact_forward(g, vol.astype(np.float64))) < 1e-5
+        pr = engine.Plan(ctx, g, "rc")
+        assert np.array_equal(pr.forward(vol), O.rc_forward(g, vol))
+
+
+def test_single_view_forward(ctx):
+    g = small_geoms()[0]
+    vol = phantom_for(g)
+    for fam in ("rc", "exact"):
+        plan = engine.Plan(ctx, g, fam)
+        full = plan.forward(vol)
+        one = plan.forward_single(vol, g.src[2], g.det_origin[2])
+        if fam == "rc":
+            assert np.array_equal(one, full[2])
+        else:
+            assert rel_l2(one, full[2]) < 1e-6
+
+
+def test_invalid_arguments_return_status(ctx):
+    g = small_geoms()[0]
+    bad = Geometry(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, g.nu, g.nv, g.du, g.dv,
+                   g.src * np.array([1, 1, -1], np.float32), g.det_origin, g.fulcrum_z)
+    with pytest.raises(KvError) as e:
+        engine.Plan(ctx, bad, "exact")          # source below the volume
+    assert e.value.status == 2
+    with pytest.raises(KvError) as e:
+        engine.Plan(ctx, g, "rc", "bf16")
+    assert e.value.status == 7
+    plan = engine.Plan(ctx, g, "exact")
+    with pytest.raises(ValueError):
+        plan.forward(np.zeros(5, np.float32))
+
+
+def test_chest_scale_exact_properties(ctx):
+    """Size-independent checks at the chest-DT geometry (1024^2 x 128 volume,
+    60 views of 2048^2): dot-product identity with FP64 reductions, and A 1 equal
+    to the chord lengths of a sample of rays from the FP64 oracle."""
+    torch = pytest.importorskip("torch")
+    g = config_chest()
+    plan = engine.Plan(ctx, g, "exact")
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.rand(g.volume_shape, generator=gen, device="cuda")
+    y = torch.rand(g.proj_shape, generator=gen, device="cuda")
+    ax = plan.forward(x)
+    aty = plan.back(y)
+    lhs = torch.dot(ax.double().flatten(), y.double().flatten()).item()
+    rhs = torch.dot(x.double().flatten(), aty.double().flatten()).item()
+    assert abs(lhs - rhs) <= DOT_REL * abs(lhs)
+    ones = torch.ones(g.volume_shape, device="cuda")
+    a1 = plan.forward(ones).cpu().numpy().reshape(-1)
+    rays = np.random.default_rng(0).integers(0, g.n_rays, 20000)
+    assert rel_l2(a1[rays], chord_lengths(g, rays)) < 1e-5
+
+
+def chord_lengths(g, rays):
+    """FP64 length of each ray inside the volume box (slab method)."""
+    view = rays // (g.nu * g.nv)
+    v = (rays // g.nu) % g.nv
+    u = rays % g.nu
+    s = g.src[view].astype(np.float64)
+    p = g.det_origin[view].astype(np.float64)
+    p[:, 0] += (u + 0.5) * np.float64(g.du)
+    p[:, 1] += (v + 0.5) * np.float64(g.dv)
+    d = p - s
+    half = 0.5 * np.array([g.nx * g.dx, g.ny * g.dy, g.nz * g.dz])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t0 = (-half - s) / d
+        t1 = (half - s) / d
+    lo = np.maximum(0.0, np.minimum(t0, t1).max(axis=1))
+    hi = np.minimum(1.0, np.maximum(t0, t1).min(axis=1))
+    return np.maximum(hi - lo, 0.0) * np.linalg.norm(d, axis=1)

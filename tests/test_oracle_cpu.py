@@ -1,0 +1,168 @@
+"""CPU tests of the oracle itself: pinned against the reference kernels (run
+here when the reference tree is present, and through the committed golden
+fixtures everywhere) and against known answers for the FP64 Siddon."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from kevernals_gb300 import phantom as ph
+from kevernals_gb300.geometry import Geometry, config_small, linear_sweep
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load_small():
+    z = np.load(os.path.join(GOLDEN, "golden_small.npz"))
+    cases = {}
+    for name in ("a", "b", "c"):
+        nx, ny, nz, nu, nv = (int(t) for t in z[f"{name}_dims"])
+        dx, dy, dz, du, dv, fz = (float(t) for t in z[f"{name}_spacing"])
+        g = Geometry(nx, ny, nz, dx, dy, dz, nu, nv, du, dv, z[f"{name}_src"], z[f"{name}_det"], fz)
+        cases[name] = (g, {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "_")})
+    return cases
+
+
+@pytest.mark.parametrize("name", ["a", "b", "c"])
+def test_rc_oracle_matches_reference_golden(name):
+    g, d = load_small()[name]
+    vol = O.phantom(g, d["params"])
+    assert np.array_equal(vol, d["vol"])
+    assert np.array_equal(O.rc_forward(g, vol), d["fwd"])          # bit-exact
+    assert np.array_equal(O.rc_back(g, d["fwd"]), d["back"])
+    assert np.array_equal(O.rc_back(g, d["y"]), d["back_y"])
+
+
+def test_golden_covers_missed_rays_and_single_view():
+    cases = load_small()
+    g, d = cases["b"]
+    assert (d["fwd"] == 0).any() and (d["fwd"] > 0).any()
+    g, d = cases["c"]
+    assert g.n_views == 1
+
+
+@pytest.mark.skipif(O.ref_lib() is None, reason="reference tree not present")
+def test_rc_oracle_matches_reference_kernels_random():
+    rng = np.random.default_rng(7)
+    for trial in range(3):
+        nx, ny, nz = rng.integers(8, 30, 3)
+        g = linear_sweep(int(nx), int(ny), int(nz), 0.5, 0.6, 1.1, int(rng.integers(2, 6)),
+                         int(rng.integers(10, 40)), int(rng.integers(10, 40)), 0.45, 0.5,
+                         float(rng.uniform(5, 25)))
+        vol = rng.random(g.volume_shape, dtype=np.float32)
+        f_ref = O.ref_forward(g, vol)
+        assert np.array_equal(O.rc_forward(g, vol), f_ref)
+        assert np.array_equal(O.rc_back(g, f_ref), O.ref_back(g, f_ref))
+
+
+def test_rc_uniform_volume_known_answer():
+    # the reference forward is a path-length weighted mean: 1 on every hitting ray
+    g = linear_sweep(20, 20, 8, 0.5, 0.5, 1.0, 3, 30, 30, 0.4, 0.4, 10.0)
+    f = O.rc_forward(g, np.ones(g.volume_shape, np.float32))
+    assert set(np.unique(f)) <= {0.0, 1.0}
+    assert (f == 1.0).mean() > 0.5
+
+
+def _chord(g, view, u, v):
+    """Analytic length of the ray (u, v) inside the volume box (slab method)."""
+    s = g.src[view].astype(np.float64)
+    p = g.det_origin[view].astype(np.float64) + np.array([(u + .5) * g.du, (v + .5) * g.dv, 0])
+    d = p - s
+    half = 0.5 * np.array([g.nx * g.dx, g.ny * g.dy, g.nz * g.dz])
+    lo, hi = 0.0, 1.0
+    for a in range(3):
+        if d[a] == 0:
+            if not (-half[a] <= s[a] < half[a]):
+                return 0.0
+            continue
+        t0, t1 = sorted(((-half[a] - s[a]) / d[a], (half[a] - s[a]) / d[a]))
+        lo, hi = max(lo, t0), min(hi, t1)
+    return max(0.0, hi - lo) * np.linalg.norm(d)
+
+
+def test_exact_oracle_chord_lengths():
+    g = linear_sweep(16, 14, 6, 0.5, 0.5, 1.0, 3, 24, 22, 0.5, 0.5, 20.0)
+    f = O.exact_forward(g, np.full(g.volume_shape, 2.0))
+    for view in range(3):
+        for (u, v) in [(0, 0), (5, 7), (12, 11), (23, 21)]:
+            assert f[view, v, u] == pytest.approx(2.0 * _chord(g, view, u, v), rel=1e-12, abs=1e-12)
+    assert np.allclose(O.exact_ray_lengths(g), f / 2.0, rtol=1e-12, atol=1e-12)
+
+
+def test_exact_oracle_impulse_response():
+    g = linear_sweep(9, 9, 5, 1.0, 1.0, 1.0, 2, 20, 20, 0.7, 0.7, 12.0)
+    vol = np.zeros(g.volume_shape)
+    vol[2, 4, 4] = 1.0
+    f = O.exact_forward(g, vol)
+    # the impulse response of each ray is its chord through the voxel box
+    box_lo = np.array([4 * 1.0 - 4.5, 4 * 1.0 - 4.5, 2 * 1.0 - 2.5])
+    for view in range(2):
+        for v in range(20):
+            for u in range(20):
+                s = g.src[view].astype(np.float64)
+                p = g.det_origin[view].astype(np.float64) + np.array([(u + .5) * np.float64(g.du), (v + .5) * np.float64(g.dv), 0])
+                d = p - s
+                lo, hi = 0.0, 1.0
+                for a in range(3):
+                    t0, t1 = sorted(((box_lo[a] - s[a]) / d[a], (box_lo[a] + 1 - s[a]) / d[a]))
+                    lo, hi = max(lo, t0), min(hi, t1)
+                want = max(0.0, hi - lo) * np.linalg.norm(d)
+                assert f[view, v, u] == pytest.approx(want, abs=1e-12)
+
+
+def test_exact_oracle_is_a_transpose():
+    g = linear_sweep(12, 10, 6, 0.5, 0.5, 1.0, 4, 18, 16, 0.4, 0.4, 15.0)
+    rng = np.random.default_rng(3)
+    x = rng.random(g.volume_shape)
+    y = rng.random(g.proj_shape)
+    lhs = np.vdot(O.exact_forward(g, x), y)
+    rhs = np.vdot(x, O.exact_back(g, y))
+    assert abs(lhs - rhs) <= 1e-13 * abs(lhs)
+
+
+def test_exact_oracle_mlem_decreases_residual():
+    g = linear_sweep(16, 16, 6, 0.5, 0.5, 1.0, 5, 24, 24, 0.4, 0.4, 15.0)
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 5, ph.seed_for(0, 1))
+    truth = O.phantom(g, params).astype(np.float64)
+    p = O.exact_forward(g, truth)
+    res = []
+    x = np.ones(g.volume_shape)
+    for k in range(4):
+        res.append(np.linalg.norm(O.exact_forward(g, x) - p) / np.linalg.norm(p))
+        x = O.exact_mlem(g, p, x, 2)
+    assert all(b < a for a, b in zip(res, res[1:]))
+    assert (x >= 0).all()
+
+
+def test_saa_shift_rules():
+    g = config_small()
+    rc = O.saa_shifts(g, 0)
+    ex = O.saa_shifts(g, 1)
+    assert rc.shape == ex.shape == (g.nz, g.n_views)
+    # central view (source y = 0) is never shifted
+    assert (rc[:, g.n_views // 2] == 0).all() and (ex[:, g.n_views // 2] == 0).all()
+    # shifts are odd in the source position
+    assert np.array_equal(ex[:, 0], -ex[:, -1])
+
+
+def test_splitmix64_known_values():
+    # first outputs of splitmix64 seeded with 0 (published reference sequence)
+    r = ph.SplitMix64(0)
+    assert r.next_u64() == 0xE220A8397B1DCDAF
+    assert r.next_u64() == 0x6E789E6AA1B965F4
+    a = ph.ellipsoid_params(64, 64, 16, 0.5, 0.5, 1.0, 10, 123)
+    b = ph.ellipsoid_params(64, 64, 16, 0.5, 0.5, 1.0, 10, 123)
+    assert np.array_equal(a, b) and a.shape == (11, 16)
+
+
+def test_config1_digests_from_reference():
+    info = json.load(open(os.path.join(GOLDEN, "golden_config1.json")))
+    g = config_small()
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 40, info["seed"])
+    vol = O.phantom(g, params)
+    d = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    assert d(vol) == info["phantom_sha256"]
+    assert d(O.rc_forward(g, vol)) == info["ref_forward_sha256"]
