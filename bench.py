@@ -1,0 +1,376 @@
+#!/usr/bin/env python
+"""Chest-DT MLEM benchmark of the kvtomo engine (one JSON line on stdout).
+
+Workload (default): the chest-DT acquisition -- volume 1024x1024x128 at
+0.4x0.4x2.5 mm, 60 views over +-17.5 deg, 2048^2 detector at 0.2 mm,
+SID 1000 mm, SOD 850 mm -- with a seeded 400-ellipsoid phantom and Poisson
+data at I0 = 5e4 (synthetic: no dataset is involved).  One step = one plain
+MLEM iteration from the uniform start (forward projection with the fused
+ratio, backprojection with the fused multiplicative update).
+
+  value      projector rays/s = 2 * P * D rays (A and A^T) per iteration,
+             inputs resident in HBM, CUDA events on the launching stream.
+  e2e        the same metric through the C ABI with HOST buffers: every step
+             copies the projections and the iterate in and the iterate out.
+  roofline   the dominant kernel's algorithmic bytes per launch over its
+             live average duration (per-launch CUDA events), against the
+             measured HBM copy bandwidth.
+  cpu_baseline  the oracle (FP64 Siddon, all host cores) on a bounded sample
+             of rays of the same workload, extrapolated to the metric.
+
+--impl reference times the reference's own CPU path for the same metric:
+its MLEM iteration (reference-compatible forward with the reference's
+selection sort, windowed backprojector, host ratio/update loops, as restated
+in oracle/) on sampled rays and voxels of the same workload, all host cores.
+
+Multi-GPU (torchrun): replicas only -- each rank solves its own seeded case;
+value = all ranks' rays / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "chest-DT time-to-residual (learned vs plain GPU MLEM); projector rays/s, %HBM"
+UNIT = "rays/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["kvtomo", "reference"], default="kvtomo")
+    ap.add_argument("--family", choices=["exact", "rc"], default="exact")
+    ap.add_argument("--storage", choices=["f32", "bf16", "f16"], default="f32")
+    ap.add_argument("--workload", choices=["chest", "small"], default="chest")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def geometry(workload):
+    from kevernals_gb300.geometry import config_chest, config_small
+    if workload == "chest":
+        return config_chest(), 400, 5e4, 2, (
+            "chest-DT: 1024x1024x128 @ 0.4x0.4x2.5 mm, 60 views +-17.5 deg, 2048^2 @ 0.2 mm, "
+            "SID 1000 / SOD 850 mm")
+    return config_small(), 40, 1e4, 1, (
+        "small: 256x256x64 @ 0.5x0.5x1.0 mm, 15 views +-15 deg, 512^2 @ 0.4 mm")
+
+
+# ----------------------------------------------------------------- helpers
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = open(os.devnull if False else "/tmp/kv_clocks_%d.csv" % os.getpid(), "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.out.name):
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.out.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel, workload):
+    """DRAM traffic per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(path))
+        return d[workload][kernel]["bytes_per_launch"]
+    except Exception:
+        return None
+
+
+def algorithmic_bytes(kernel, g, sv, sp):
+    """Compulsory bytes of one launch (every input read once, every output
+    written once) for the fused MLEM kernels."""
+    V, PD = g.n_voxels, g.n_rays
+    return {
+        "exact_fwd": sv * V + 2 * sp * PD,            # read x, p; write ratio
+        "exact_back": sp * PD + 2 * sv * V + 8 * V,   # read ratio; read+write x; read FP64 sens
+        "rc_fwd": 4 * V + 8 * PD,
+        "rc_back": 4 * PD + 8 * V,
+    }.get(kernel)
+
+
+# ---------------------------------------------------------------- the arms
+
+def cpu_baseline_exact(g, truth_np, p_np, seconds, seed=0):
+    """FP64 oracle forward + transpose on a bounded sample of rays, all
+    host cores; extrapolated to rays/s of the MLEM iteration."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    vol64 = truth_np.astype(np.float64)
+    back = np.zeros(g.volume_shape, np.float64)
+    n = 2000
+    while True:
+        rays = rng.integers(0, g.n_rays, n)
+        t0 = time.perf_counter()
+        O.exact_forward_rays(g, vol64, rays)
+        t1 = time.perf_counter()
+        O.exact_back_rays(g, p_np.reshape(-1)[rays].astype(np.float64), rays, back)
+        t2 = time.perf_counter()
+        if t2 - t0 > 0.25 * seconds or n >= 1 << 22:
+            break
+        n = int(n * min(16.0, max(2.0, 0.3 * seconds / max(t2 - t0, 1e-3))))
+    rate = 2 * n / (t2 - t0)
+    return {"value": rate, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{n} random rays of the workload: FP64 Siddon forward ({t1 - t0:.2f} s) and "
+                      f"transpose ({t2 - t1:.2f} s); rate = 2 * rays / time"}
+
+
+def reference_arm(args, g, desc):
+    """The reference's MLEM iteration on the host cores, sampled."""
+    from kevernals_gb300 import phantom as ph
+    from oracle import oracle as O
+    _, n_ell, i0, cfg, _ = geometry(args.workload)
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ell, ph.seed_for(cfg))
+    truth = O.phantom(g, params)
+    rng = np.random.default_rng(1)
+    proj = np.zeros(g.proj_shape, np.float32)
+    nr, nv = 256, 256
+
+    def one_step():
+        rays = rng.integers(0, g.n_rays, nr)
+        vox = rng.integers(0, g.n_voxels, nv)
+        t0 = time.perf_counter()
+        O.rc_forward_rays_refcost(g, truth, rays)
+        t1 = time.perf_counter()
+        O.rc_back_voxels(g, proj, vox)
+        t2 = time.perf_counter()
+        # full iteration time: all rays, all voxels, plus the host ratio and update loops
+        t_iter = (t1 - t0) * g.n_rays / nr + (t2 - t1) * g.n_voxels / nv
+        return t_iter, t2 - t0
+
+    # size the samples to about two seconds of host work per step
+    for _ in range(3):
+        t_iter, wall = one_step()
+        if wall > 1.0:
+            break
+        nr, nv = nr * 4, nv * 4
+    iters = []
+    for _ in range(args.warmup):
+        one_step()
+    for _ in range(args.steps):
+        iters.append(one_step()[0])
+    t_iter = statistics.mean(iters)
+    value = 2 * g.n_rays / t_iter
+    cores = O.num_threads()
+    sample = (f"per step {nr} random rays (forward, reference selection sort) and {nv} random voxels "
+              f"(11x11-window backprojector) of the workload, extrapolated to one MLEM iteration "
+              f"({t_iter:.1f} s)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded ellipsoid phantom", "config": {"workload": desc, "family": "rc",
+                                                                       "step": "one MLEM iteration"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
+    import torch
+
+    from kevernals_gb300 import engine, phantom as ph
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = engine.Context(dev)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    # data: seeded phantom, EXACT line integrals, Poisson counts
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ell, ph.seed_for(cfg, rank))
+    truth = engine.phantom(ctx, g, params, device=True)
+    gen_plan = engine.Plan(ctx, g, "exact")
+    line = gen_plan.forward(truth)
+    gen = torch.Generator(device=f"cuda:{dev}").manual_seed(ph.seed_for(cfg, rank))
+    counts = torch.poisson(i0 * torch.exp(-line.double()), generator=gen)
+    p = torch.log(i0 / counts.clamp_min(1.0)).clamp_min(0.0).float().contiguous()
+    del counts, line
+    gen_plan.close()
+
+    plan = engine.Plan(ctx, g, args.family, args.storage)
+    x = plan.uniform_volume(device=True)
+    for _ in range(args.warmup):
+        plan.mlem(p, x, 1)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- timed region: device-resident inputs (both larger than L2)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    ctx.set_timing(True)
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.mlem(p, x, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    kernels = ctx.read_timing()
+    ctx.set_timing(False)
+    clocks = sampler.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    rays_per_step = 2 * g.n_rays
+    value = world * rays_per_step * args.steps / (ms * 1e-3)
+    gpu_launches = sum(n for n, _ in kernels.values())
+
+    # ---- roofline of the dominant kernel
+    sv = sp = 2 if args.storage != "f32" else 4
+    dom = max(kernels.items(), key=lambda kv: kv[1][1])[0] if kernels else None
+    roof = None
+    if dom is not None:
+        n, tot = kernels[dom]
+        byt = algorithmic_bytes(dom, g, sv, sp)
+        peak, src = measured_hbm()
+        if byt is not None:
+            ach = byt / (tot / n * 1e-3) / 1e9
+            roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "peak_source": src, "algorithmic_bytes": byt,
+                    "traffic": committed_traffic(dom, args.workload), "avg_ms": tot / n}
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        ph_p = torch.empty(g.proj_shape, dtype=torch.float32).pin_memory()
+        ph_x = torch.empty(g.volume_shape, dtype=torch.float32).pin_memory()
+        ph_p.copy_(p.cpu())
+        hp, hx = ph_p.numpy(), ph_x.numpy()
+        hx[...] = 1.0
+        plan.mlem(hp, hx, 1)          # warm the staging buffers
+        barrier()
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            plan.mlem(hp, hx, 1)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ems = a0.elapsed_time(a1)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ems], device=f"cuda:{dev}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": world * rays_per_step * args.steps / (ems * 1e-3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * (g.n_rays + g.n_voxels), "d2h_bytes_per_step": 4 * g.n_voxels,
+               "ms_per_step": ems / args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline_exact(g, truth.cpu().numpy(), p.cpu().numpy(), args.cpu_seconds)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.storage == "f32" else args.storage,
+            "data": f"synthetic: seeded {n_ell}-ellipsoid phantom, EXACT line integrals, Poisson I0={i0:g}",
+            "config": {"workload": desc, "family": args.family, "storage": args.storage,
+                       "step": "one MLEM iteration (forward+ratio, backprojection+update)",
+                       "rays_per_step": rays_per_step, "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": gpu_launches, "roofline": roof,
+            "cpu_baseline": cpu,
+            "kernels": {k: {"launches": n, "avg_ms": t / n} for k, (n, t) in kernels.items()},
+        }
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    g, n_ell, i0, cfg, desc = geometry(args.workload)
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, g, desc)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    try:
+        gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

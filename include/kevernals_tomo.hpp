@@ -1,0 +1,436 @@
+// kevernals_tomo.hpp -- C++ drop-in for the Kevernals projection /
+// reconstruction modules, over the kvtomo C ABI (kvtomo.h).
+//
+// Same names, argument meaning and error behaviour as the reference:
+//   Projector               source/modules/reconstruction/Projector.h:10-28
+//   recons::ART / MLEM / BackProjection / ShiftAndAdd
+//                           source/modules/reconstruction/Reconstructors.h:19-379
+//   ReconstructorsErrorCode source/modules/reconstruction/ReconstructorsErrorCode.h:19-26
+//   Result<T>               source/commons/Result.h:17-41 (value or std::error_code)
+//   TomoGeometry accessors  source/modules/geometry/TomoGeometry.h:34-89
+// Differences, by design:
+//   * ImageDataPtr is a small reference-counted headless image (dimensions,
+//     spacing, origin, float32 buffer) instead of vtkSmartPointer<vtkImageData>.
+//   * TomoGeometry is built from values (the XML reader is not part of this
+//     layer); it keeps the reference's conventions: volume-centred frame,
+//     common source x/z and detector z, one ROI size and pixel spacing.
+//   * Projector takes an operator family: KV_FAMILY_RC (default) reproduces
+//     the reference kernels; KV_FAMILY_EXACT is the Siddon line integral and
+//     its exact transpose.
+//   * Errors never exit the process: CUDA failures surface as error codes.
+//   * All functions are inline (the reference defines them in a header
+//     without `inline`).
+#pragma once
+
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <memory>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <system_error>
+#include <vector>
+
+#include "kvtomo.h"
+
+// ---------------------------------------------------------------- values
+
+struct Position2D {
+    float x = 0.f, y = 0.f;
+};
+struct Position3D {
+    float x = 0.f, y = 0.f, z = 0.f;
+};
+struct Size2D {
+    int x = 0, y = 0;
+};
+struct Size3D {
+    int x = 0, y = 0, z = 0;
+};
+struct PixelSpacing {
+    float x = 0.f, y = 0.f;
+};
+struct VoxelSpacing {
+    float x = 0.f, y = 0.f, z = 0.f;
+};
+using WSize3D = Position3D;
+
+// ---------------------------------------------------------------- errors
+
+enum class ReconstructorsErrorCode { ART = 1, BackProjectionFailed, ProjectionFailed, MLEM, ShiftAndAdd };
+
+namespace kvtomo_detail {
+class ReconstructorsCategory : public std::error_category {
+public:
+    const char *name() const noexcept override { return "Reconstructors"; }
+    std::string message(int c) const override {
+        switch (static_cast<ReconstructorsErrorCode>(c)) {
+        case ReconstructorsErrorCode::ART: return "ART reconstruction failed";
+        case ReconstructorsErrorCode::BackProjectionFailed: return "back projection failed";
+        case ReconstructorsErrorCode::ProjectionFailed: return "projection failed";
+        case ReconstructorsErrorCode::MLEM: return "MLEM reconstruction failed";
+        case ReconstructorsErrorCode::ShiftAndAdd: return "shift and add failed";
+        }
+        return "unknown reconstructors error";
+    }
+};
+inline const std::error_category &reconstructors_category() {
+    static ReconstructorsCategory c;
+    return c;
+}
+}  // namespace kvtomo_detail
+
+namespace std {
+template <> struct is_error_code_enum<ReconstructorsErrorCode> : public true_type {};
+}  // namespace std
+
+inline std::error_code make_error_code(ReconstructorsErrorCode e) {
+    return {static_cast<int>(e), kvtomo_detail::reconstructors_category()};
+}
+
+// Value-or-error, the subset of outcome::result the reference uses.
+template <typename T> class Result {
+public:
+    Result(T v) : m_value(std::move(v)) {}
+    Result(std::error_code e) : m_error(e) {}
+    Result(ReconstructorsErrorCode e) : m_error(make_error_code(e)) {}
+    bool has_value() const { return !m_error; }
+    bool has_error() const { return static_cast<bool>(m_error); }
+    explicit operator bool() const { return has_value(); }
+    const T &value() const {
+        if (m_error) throw std::system_error(m_error);
+        return m_value;
+    }
+    T &value() {
+        if (m_error) throw std::system_error(m_error);
+        return m_value;
+    }
+    std::error_code error() const { return m_error; }
+
+private:
+    T m_value{};
+    std::error_code m_error{};
+};
+
+// ---------------------------------------------------------------- images
+
+class ImageData {
+public:
+    static std::shared_ptr<ImageData> New() { return std::make_shared<ImageData>(); }
+    void SetDimensions(int x, int y, int z) {
+        m_dims[0] = x;
+        m_dims[1] = y;
+        m_dims[2] = z;
+    }
+    int *GetDimensions() { return m_dims; }
+    const int *GetDimensions() const { return m_dims; }
+    void SetSpacing(double x, double y, double z) {
+        m_spacing[0] = x;
+        m_spacing[1] = y;
+        m_spacing[2] = z;
+    }
+    void GetSpacing(double out[3]) const {
+        for (int i = 0; i < 3; ++i) out[i] = m_spacing[i];
+    }
+    void SetOrigin(double x, double y, double z) {
+        m_origin[0] = x;
+        m_origin[1] = y;
+        m_origin[2] = z;
+    }
+    void GetOrigin(double out[3]) const {
+        for (int i = 0; i < 3; ++i) out[i] = m_origin[i];
+    }
+    // VTK_FLOAT with one component is the only scalar type used on this path.
+    void AllocateScalars(int = 0, int = 1) { m_data.assign(size(), 0.f); }
+    void *GetScalarPointer() { return m_data.data(); }
+    const float *data() const { return m_data.data(); }
+    float *data() { return m_data.data(); }
+    size_t size() const { return (size_t)m_dims[0] * m_dims[1] * m_dims[2]; }
+
+private:
+    int m_dims[3] = {0, 0, 0};
+    double m_spacing[3] = {1, 1, 1};
+    double m_origin[3] = {0, 0, 0};
+    std::vector<float> m_data;
+};
+using ImageDataPtr = std::shared_ptr<ImageData>;
+
+// ---------------------------------------------------------------- geometry
+
+class TomoGeometry {
+public:
+    // volume: voxel counts and spacing, centred at the origin
+    // sources: per-view positions (their x and z are averaged, as TomoTable
+    //          does, TomoTable.cpp:4-19)
+    // roiBottomLeft: per-view ROI bottom-left corner (x, y); detectorZ: one plane
+    // roiSize / pixelSpacing: ROI pixel counts and pitch; fulcrum: rotation centre
+    TomoGeometry(Size3D volumeSize, VoxelSpacing spacing, const std::vector<Position3D> &sources,
+                 const std::vector<Position2D> &roiBottomLeft, float detectorZ, Size2D roiSize,
+                 PixelSpacing pixelSpacing, WSize3D fulcrum = {})
+        : m_size(volumeSize), m_spacing(spacing), m_roiBL(roiBottomLeft), m_roiSize(roiSize),
+          m_pixel(pixelSpacing), m_fulcrum(fulcrum), m_detZ(detectorZ) {
+        if (sources.size() != roiBottomLeft.size() || sources.empty())
+            throw std::invalid_argument("TomoGeometry: one source and one ROI origin per view");
+        float sx = 0.f, sz = 0.f;
+        for (const auto &s : sources) {
+            sx += s.x;
+            m_srcY.push_back(s.y);
+            sz += s.z;
+        }
+        m_srcX = sx / static_cast<float>(sources.size());
+        m_srcZ = sz / static_cast<float>(sources.size());
+        m_valid = true;
+    }
+    bool IsValid() const { return m_valid; }
+
+    std::vector<float> sourcesYPositions() const { return m_srcY; }
+    float sourcesXCommonPosition() const { return m_srcX; }
+    float sourcesZCommonPosition() const { return m_srcZ; }
+    float detectorsZCommonPosition() const { return m_detZ; }
+    float sid() const { return std::abs(m_detZ - m_srcZ); }
+    int nbProjections() const { return static_cast<int>(m_srcY.size()); }
+    int nbProjectionsRois() const { return nbProjections(); }
+    std::vector<Position2D> projectionsRoisBottomLeftPositions() const { return m_roiBL; }
+    Size2D projectionsRoisSize() const { return m_roiSize; }
+    PixelSpacing projectionsPixelSpacing() const { return m_pixel; }
+    PixelSpacing projectionsRoisPixelSpacing() const { return m_pixel; }
+    Size3D volumeSize3D() const { return m_size; }
+    VoxelSpacing volumeVoxelSpacing() const { return m_spacing; }
+    Position3D volumeBLF() const {
+        return {-0.5f * m_size.x * m_spacing.x, -0.5f * m_size.y * m_spacing.y, -0.5f * m_size.z * m_spacing.z};
+    }
+    WSize3D fulcrum() const { return m_fulcrum; }
+
+    // Flattened description the kernels consume (Projector.cu:917-940):
+    // sources (common x, y_i, common z), ROI origins (x_i, y_i, common z).
+    struct Flat {
+        kv_geometry g;
+        std::vector<float> src, det;
+    };
+    std::shared_ptr<Flat> flatten() const {
+        auto f = std::make_shared<Flat>();
+        const int P = nbProjections();
+        f->src.resize(3 * P);
+        f->det.resize(3 * P);
+        for (int i = 0; i < P; ++i) {
+            f->src[3 * i] = m_srcX;
+            f->src[3 * i + 1] = m_srcY[i];
+            f->src[3 * i + 2] = m_srcZ;
+            f->det[3 * i] = m_roiBL[i].x;
+            f->det[3 * i + 1] = m_roiBL[i].y;
+            f->det[3 * i + 2] = m_detZ;
+        }
+        f->g = kv_geometry{m_size.x, m_size.y, m_size.z, m_spacing.x, m_spacing.y, m_spacing.z, P,
+                           m_roiSize.x, m_roiSize.y, m_pixel.x, m_pixel.y, f->src.data(), f->det.data(),
+                           m_fulcrum.z};
+        return f;
+    }
+
+private:
+    Size3D m_size;
+    VoxelSpacing m_spacing;
+    std::vector<float> m_srcY;
+    float m_srcX = 0.f, m_srcZ = 0.f;
+    std::vector<Position2D> m_roiBL;
+    Size2D m_roiSize;
+    PixelSpacing m_pixel;
+    WSize3D m_fulcrum;
+    float m_detZ = 0.f;
+    bool m_valid = false;
+};
+
+// ---------------------------------------------------------------- engine
+
+namespace kvtomo_detail {
+// One context per host thread, created on first use.
+inline kv_ctx *thread_context() {
+    struct Holder {
+        kv_ctx *ctx = nullptr;
+        ~Holder() {
+            if (ctx) kv_ctx_destroy(ctx);
+        }
+    };
+    thread_local Holder h;
+    if (h.ctx == nullptr) {
+        const char *dev = std::getenv("KVTOMO_DEVICE");
+        if (kv_ctx_create(dev ? std::atoi(dev) : 0, &h.ctx) != KV_OK) h.ctx = nullptr;
+    }
+    return h.ctx;
+}
+
+struct PlanHandle {
+    kv_plan *plan = nullptr;
+    ~PlanHandle() {
+        if (plan) kv_plan_destroy(plan);
+    }
+};
+
+inline std::shared_ptr<PlanHandle> make_plan(const TomoGeometry *g, kv_family family,
+                                              kv_storage storage = KV_STORAGE_F32) {
+    kv_ctx *ctx = thread_context();
+    if (ctx == nullptr || g == nullptr) return nullptr;
+    auto flat = g->flatten();
+    auto h = std::make_shared<PlanHandle>();
+    if (kv_plan_create(ctx, &flat->g, family, storage, &h->plan) != KV_OK) return nullptr;
+    return h;
+}
+
+inline void write_raw(const std::string &path, const ImageDataPtr &img) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char *>(img->data()), (std::streamsize)(img->size() * sizeof(float)));
+}
+}  // namespace kvtomo_detail
+
+class Projector {
+public:
+    explicit Projector(TomoGeometry *p_tomoGeometry, kv_family family = KV_FAMILY_RC)
+        : m_tomoGeometry(p_tomoGeometry), m_family(family) {}
+
+    // Projector::PerformProjection, Projector.cu:873-1036.  Returns nullptr on failure.
+    ImageDataPtr PerformProjection(ImageDataPtr p_volume) const {
+        if (!ensure() || p_volume == nullptr || p_volume->size() != kv_plan_volume_elems(m_plan->plan)) return nullptr;
+        auto out = ImageData::New();
+        const auto roi = m_tomoGeometry->projectionsRoisSize();
+        out->SetDimensions(roi.x, roi.y, m_tomoGeometry->nbProjectionsRois());
+        out->SetSpacing(m_tomoGeometry->projectionsPixelSpacing().x, m_tomoGeometry->projectionsPixelSpacing().y, 1.);
+        out->AllocateScalars();
+        if (kv_forward(m_plan->plan, p_volume->data(), out->data(), KV_MEM_HOST) != KV_OK) return nullptr;
+        return out;
+    }
+
+    // Single-view projection into an existing container (Projector.cu:823-870,
+    // unfinished in the reference): the container's ROI origin is the
+    // geometry's first ROI corner on the common detector plane.
+    void PerformProjection(const ImageDataPtr p_volume, const Position3D &p_sourcePosition,
+                           ImageDataPtr p_projectionsContainer) const {
+        if (!ensure() || p_volume == nullptr || p_projectionsContainer == nullptr) return;
+        const auto roi = m_tomoGeometry->projectionsRoisSize();
+        if (p_projectionsContainer->size() != (size_t)roi.x * roi.y) {
+            p_projectionsContainer->SetDimensions(roi.x, roi.y, 1);
+            p_projectionsContainer->AllocateScalars();
+        }
+        const auto bl = m_tomoGeometry->projectionsRoisBottomLeftPositions().front();
+        const float src[3] = {p_sourcePosition.x, p_sourcePosition.y, p_sourcePosition.z};
+        const float det[3] = {bl.x, bl.y, m_tomoGeometry->detectorsZCommonPosition()};
+        kv_forward_single(m_plan->plan, p_volume->data(), src, det, p_projectionsContainer->data(), KV_MEM_HOST);
+    }
+
+    // Projector::PerformBackProjection, Projector.cu:1038-1207.
+    ImageDataPtr PerformBackProjection(ImageDataPtr p_projections) const {
+        if (!ensure() || p_projections == nullptr || p_projections->size() != kv_plan_proj_elems(m_plan->plan))
+            return nullptr;
+        auto out = ImageData::New();
+        const auto n = m_tomoGeometry->volumeSize3D();
+        const auto s = m_tomoGeometry->volumeVoxelSpacing();
+        out->SetDimensions(n.x, n.y, n.z);
+        out->SetSpacing(s.x, s.y, s.z);
+        out->AllocateScalars();
+        if (kv_back(m_plan->plan, p_projections->data(), out->data(), KV_MEM_HOST) != KV_OK) return nullptr;
+        return out;
+    }
+
+    kv_plan *plan() const { return ensure() ? m_plan->plan : nullptr; }
+
+private:
+    bool ensure() const {
+        if (!m_plan) m_plan = kvtomo_detail::make_plan(m_tomoGeometry, m_family);
+        return m_plan != nullptr;
+    }
+    TomoGeometry *m_tomoGeometry;
+    kv_family m_family;
+    mutable std::shared_ptr<kvtomo_detail::PlanHandle> m_plan;
+};
+
+namespace recons {
+
+namespace detail {
+inline ImageDataPtr uniform_volume(const TomoGeometry *g) {
+    // PhantomMaker(volume, 1.f).GetPhantom(): background density 1 everywhere
+    auto v = ImageData::New();
+    const auto n = g->volumeSize3D();
+    const auto s = g->volumeVoxelSpacing();
+    v->SetDimensions(n.x, n.y, n.z);
+    v->SetSpacing(s.x, s.y, s.z);
+    v->AllocateScalars();
+    for (size_t i = 0; i < v->size(); ++i) v->data()[i] = 1.f;
+    return v;
+}
+
+inline Result<ImageDataPtr> iterate(bool mlem, TomoGeometry *g, ImageDataPtr proj, int iters, float relax,
+                                    std::optional<ImageDataPtr> init, std::optional<std::string> outDir,
+                                    kv_family family) {
+    // the reference reports MLEM failures with the ART code (Reconstructors.h:159,190,230)
+    const auto code = ReconstructorsErrorCode::ART;
+    ImageDataPtr x = init.has_value() ? init.value() : uniform_volume(g);
+    if (x == nullptr || proj == nullptr) return code;
+    Projector projector(g, family);
+    kv_plan *plan = projector.plan();
+    if (plan == nullptr || x->size() != kv_plan_volume_elems(plan) || proj->size() != kv_plan_proj_elems(plan))
+        return code;
+    auto run = mlem ? kv_mlem : kv_sart;
+    if (!outDir.has_value()) {
+        if (run(plan, proj->data(), x->data(), iters, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
+        return x;
+    }
+    // verbose mode: one file per iteration, as the reference writes TIFFs
+    // (Reconstructors.h:47-53, 125-131); raw float32 here.
+    kvtomo_detail::write_raw(outDir.value() + "initialVolume.raw", x);
+    for (int it = 0; it < iters; ++it) {
+        if (run(plan, proj->data(), x->data(), 1, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
+        kvtomo_detail::write_raw(outDir.value() + "reconstructionstep" + std::to_string(it) + ".raw", x);
+    }
+    return x;
+}
+}  // namespace detail
+
+// recons::ART, Reconstructors.h:19-134 (simultaneous: x += B(relax (p - A x)))
+inline Result<ImageDataPtr> ART(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
+                                int p_iterationNumber, float p_relaxationCoefficient,
+                                std::optional<ImageDataPtr> p_initialVolume,
+                                std::optional<std::string> p_outputDirectoryPath,
+                                kv_family family = KV_FAMILY_RC) {
+    return detail::iterate(false, p_tomoGeometry, p_projectionImages, p_iterationNumber, p_relaxationCoefficient,
+                           p_initialVolume, p_outputDirectoryPath, family);
+}
+
+// recons::MLEM, Reconstructors.h:136-253 (x *= B(relax p / A x))
+inline Result<ImageDataPtr> MLEM(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
+                                 int p_iterationNumber, float p_relaxationCoefficient,
+                                 std::optional<ImageDataPtr> p_initialVolume,
+                                 std::optional<std::string> p_outputDirectoryPath,
+                                 kv_family family = KV_FAMILY_RC) {
+    return detail::iterate(true, p_tomoGeometry, p_projectionImages, p_iterationNumber, p_relaxationCoefficient,
+                           p_initialVolume, p_outputDirectoryPath, family);
+}
+
+// recons::BackProjection, Reconstructors.h:256-261
+inline Result<ImageDataPtr> BackProjection(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
+                                           kv_family family = KV_FAMILY_RC) {
+    Projector projector{p_tomoGeometry, family};
+    auto out = projector.PerformBackProjection(p_projectionImages);
+    if (out == nullptr) return ReconstructorsErrorCode::BackProjectionFailed;
+    return out;
+}
+
+// recons::ShiftAndAdd, Reconstructors.h:263-379: one detector-sized slice per
+// volume slice.
+inline Result<ImageDataPtr> ShiftAndAdd(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
+                                        std::optional<std::string> p_outputDirectoryPath = std::nullopt,
+                                        kv_family family = KV_FAMILY_RC) {
+    (void)p_outputDirectoryPath;
+    if (p_tomoGeometry == nullptr || p_projectionImages == nullptr) return ReconstructorsErrorCode::ShiftAndAdd;
+    Projector projector{p_tomoGeometry, family};
+    kv_plan *plan = projector.plan();
+    if (plan == nullptr || p_projectionImages->size() != kv_plan_proj_elems(plan))
+        return ReconstructorsErrorCode::ShiftAndAdd;
+    auto out = ImageData::New();
+    const auto roi = p_tomoGeometry->projectionsRoisSize();
+    out->SetDimensions(roi.x, roi.y, p_tomoGeometry->volumeSize3D().z);
+    out->AllocateScalars();
+    if (kv_shift_and_add(plan, p_projectionImages->data(), out->data(), KV_MEM_HOST) != KV_OK)
+        return ReconstructorsErrorCode::ShiftAndAdd;
+    return out;
+}
+
+}  // namespace recons

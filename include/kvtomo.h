@@ -103,11 +103,20 @@ const char *kv_version(void);
 const char *kv_status_string(kv_status s);
 kv_status kv_ctx_create(int device, kv_ctx **out);
 kv_status kv_ctx_destroy(kv_ctx *ctx);
-/* Use `stream` (a cudaStream_t of the context's device, or NULL for the
- * context's own stream) for every later call on this context. */
+/* Use `stream` (a cudaStream_t of the context's device; NULL is the CUDA
+ * default stream) for every later call on this context.  A new context uses a
+ * stream of its own. */
 kv_status kv_ctx_set_stream(kv_ctx *ctx, void *cuda_stream);
 kv_status kv_sync(kv_ctx *ctx);
 const char *kv_ctx_last_error(const kv_ctx *ctx);
+/* Tracing (no reference counterpart: the reference prints grid sizes and the
+ * last CUDA error, Projector.cu:948-962).  While enabled, every kernel the
+ * context launches is bracketed by CUDA events on its stream.
+ * kv_ctx_timing_read synchronises the stream and writes one line per kernel
+ * name, "<name> <launches> <total device ms>", into buf (NUL-terminated,
+ * truncated to buflen), then clears the records. */
+kv_status kv_ctx_set_timing(kv_ctx *ctx, int enable);
+kv_status kv_ctx_timing_read(kv_ctx *ctx, char *buf, size_t buflen);
 
 /* ---- plans -------------------------------------------------------------- */
 /* Validates the geometry, uploads per-view tables, and keeps the workspace a

@@ -42,6 +42,8 @@ SIGNATURES = {
     "kv_ctx_set_stream": ([_vp, _vp], C.c_int),
     "kv_sync": ([_vp], C.c_int),
     "kv_ctx_last_error": ([_vp], C.c_char_p),
+    "kv_ctx_set_timing": ([_vp, C.c_int], C.c_int),
+    "kv_ctx_timing_read": ([_vp, C.c_char_p, C.c_size_t], C.c_int),
     "kv_plan_create": ([_vp, C.POINTER(KvGeometry), C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
     "kv_plan_destroy": ([_vp], C.c_int),
     "kv_plan_volume_elems": ([_vp], C.c_size_t),

@@ -188,6 +188,11 @@ extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
     if (ctx == nullptr) return KV_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (const kv_timing_rec &r : ctx->timing_recs) {
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     cudaFree(ctx->d_red);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -196,7 +201,7 @@ extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
 
 extern "C" kv_status kv_ctx_set_stream(kv_ctx *ctx, void *stream) {
     if (ctx == nullptr) return KV_ERR_INVALID_ARG;
-    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    ctx->stream = (cudaStream_t)stream;   // NULL: the CUDA default stream
     return KV_OK;
 }
 
@@ -208,6 +213,70 @@ extern "C" kv_status kv_sync(kv_ctx *ctx) {
 
 extern "C" const char *kv_ctx_last_error(const kv_ctx *ctx) {
     return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+// ---------------------------------------------------------------------------
+// Tracing
+// ---------------------------------------------------------------------------
+
+LaunchTimer::LaunchTimer(kv_ctx *c, const char *name) : ctx(c) {
+    if (ctx == nullptr || !ctx->timing) return;
+    cudaEvent_t ev[2];
+    for (int i = 0; i < 2; ++i) {
+        if (!ctx->event_pool.empty()) {
+            ev[i] = ctx->event_pool.back();
+            ctx->event_pool.pop_back();
+        } else if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+            if (i == 1) ctx->event_pool.push_back(ev[0]);
+            return;
+        }
+    }
+    rec = kv_timing_rec{name, ev[0], ev[1]};
+    cudaEventRecord(rec.start, ctx->stream);
+}
+
+LaunchTimer::~LaunchTimer() {
+    if (rec.name == nullptr) return;
+    cudaEventRecord(rec.stop, ctx->stream);
+    ctx->timing_recs.push_back(rec);
+}
+
+extern "C" kv_status kv_ctx_set_timing(kv_ctx *ctx, int enable) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    ctx->timing = enable != 0;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_ctx_timing_read(kv_ctx *ctx, char *buf, size_t buflen) {
+    if (ctx == nullptr || buf == nullptr || buflen == 0) return KV_ERR_INVALID_ARG;
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<std::string> names;
+    std::vector<double> ms;
+    std::vector<long> count;
+    for (const kv_timing_rec &r : ctx->timing_recs) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, r.start, r.stop);
+        size_t k = 0;
+        while (k < names.size() && names[k] != r.name) ++k;
+        if (k == names.size()) {
+            names.emplace_back(r.name);
+            ms.push_back(0.0);
+            count.push_back(0);
+        }
+        ms[k] += t;
+        count[k] += 1;
+        ctx->event_pool.push_back(r.start);
+        ctx->event_pool.push_back(r.stop);
+    }
+    ctx->timing_recs.clear();
+    std::string out;
+    char line[256];
+    for (size_t k = 0; k < names.size(); ++k) {
+        snprintf(line, sizeof line, "%s %ld %.6f\n", names[k].c_str(), count[k], ms[k]);
+        out += line;
+    }
+    snprintf(buf, buflen, "%s", out.c_str());
+    return KV_OK;
 }
 
 // ---------------------------------------------------------------------------

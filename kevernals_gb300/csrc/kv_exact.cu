@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T,
         float kxl, kxh, kyl, kyh;
         lateral_slices((float)ib + fmaf(X.y, hr0, X.x), X.y * dh, G.nx, G.nz, kxl, kxh);
         lateral_slices((float)jb + fmaf(Y.y, hr0, Y.x), Y.y * dh, G.ny, G.nz, kyl, kyh);
-        const float klo = fmaxf(kxl, kyl), khi = fminf(kxh, kyh);
+        // clamp in float first: converting a huge value saturates and the -1 / +1 would wrap
+        const float klo = fmaxf(fmaxf(kxl, kyl), -2.f), khi = fminf(fminf(kxh, kyh), (float)G.nz + 2.f);
         int k0 = 0, k1 = -1;
         if (klo <= khi) {
             k0 = max(0, (int)floorf(klo) - 1);
@@ -404,6 +405,7 @@ kv_status fwd_dispatch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
     dim3 block(32, plan->fwd_by);
     dim3 grid((G.nu + 31) / 32, (G.nv + plan->fwd_by - 1) / plan->fwd_by, P);
     cudaStream_t st = plan->ctx->stream;
+    LaunchTimer lt(plan->ctx, "exact_fwd");
     switch (mode) {
     case FWD_PLAIN: exact_fwd_kernel<VolT, ProjT, FWD_PLAIN><<<grid, block, 0, st>>>(G, t, a, partials); break;
     case FWD_MLEM: exact_fwd_kernel<VolT, ProjT, FWD_MLEM><<<grid, block, 0, st>>>(G, t, a, partials); break;
@@ -421,6 +423,7 @@ kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool ka
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
     cudaStream_t st = plan->ctx->stream;
     const ExactTables &t = plan->ex;
+    LaunchTimer lt(plan->ctx, "exact_back");
     if (kahan) {
         switch (mode) {
         case BACK_PLAIN: exact_back_kernel<VolT, ProjT, float, BACK_PLAIN, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
@@ -456,6 +459,7 @@ kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int P, FwdMo
     }
     if (partials != nullptr) {
         if (s == KV_OK) {
+            LaunchTimer lt(plan->ctx, "reduce_partials");
             reduce_partials_kernel<<<1, 1024, 0, plan->ctx->stream>>>(partials, nblocks, a.red);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) s = kv_fail(plan->ctx, KV_ERR_CUDA, "reduce_partials_kernel: %s", cudaGetErrorString(e));
@@ -478,6 +482,7 @@ kv_status exact_prescale_launch(kv_plan *plan, const float *y, void *yp) {
     ExGeom G = exgeom(plan, plan->g.n_views);
     dim3 block(32, 8), grid((G.nu + 31) / 32, (G.nv + 7) / 8, G.n_views);
     cudaStream_t st = plan->ctx->stream;
+    LaunchTimer lt(plan->ctx, "prescale");
     switch (plan->storage) {
     case KV_STORAGE_BF16: prescale_kernel<__nv_bfloat16><<<grid, block, 0, st>>>(G, plan->ex, y, (__nv_bfloat16 *)yp); break;
     case KV_STORAGE_F16: prescale_kernel<__half><<<grid, block, 0, st>>>(G, plan->ex, y, (__half *)yp); break;
@@ -496,12 +501,16 @@ kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
     KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&ls, plan->nproj * sizeof(float), st));
     {
         dim3 block(32, 8), grid((G.nu + 31) / 32, (G.nv + 7) / 8, G.n_views);
+        LaunchTimer lt(plan->ctx, "prescale");
         prescale_kernel<float><<<grid, block, 0, st>>>(G, plan->ex, nullptr, ls);
     }
     BackArgs a{ls, nullptr, nullptr, 1.f};
     dim3 block(32, plan->back_by);
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
-    exact_back_kernel<float, float, double, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
+    {
+        LaunchTimer lt(plan->ctx, "exact_back_sens_f64");
+        exact_back_kernel<float, float, double, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
+    }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(ls, st);
     if (e != cudaSuccess) return kv_fail(plan->ctx, KV_ERR_CUDA, "sensitivity launch: %s", cudaGetErrorString(e));

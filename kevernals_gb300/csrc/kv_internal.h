@@ -16,6 +16,11 @@
 // Context and plan
 // ---------------------------------------------------------------------------
 
+struct kv_timing_rec {
+    const char *name;
+    cudaEvent_t start, stop;
+};
+
 struct kv_ctx {
     int device = 0;
     int sm_count = 0;
@@ -23,6 +28,19 @@ struct kv_ctx {
     cudaStream_t own_stream = nullptr;
     std::string last_error;
     double *d_red = nullptr;         // 8 doubles for FP64 reductions
+    // per-kernel tracing (kv_ctx_set_timing)
+    bool timing = false;
+    std::vector<kv_timing_rec> timing_recs;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+// Brackets one kernel launch with CUDA events on the context stream when the
+// context's tracing is enabled; a no-op otherwise.
+struct LaunchTimer {
+    kv_ctx *ctx;
+    kv_timing_rec rec{nullptr, nullptr, nullptr};
+    LaunchTimer(kv_ctx *c, const char *name);
+    ~LaunchTimer();
 };
 
 // Per-view geometry tables of the EXACT family, computed on the host in

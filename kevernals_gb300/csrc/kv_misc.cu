@@ -162,12 +162,14 @@ kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, f
     dim3 block(32, 8), grid((g.nu + 31) / 32, (g.nv + 7) / 8, (g.nz + kb - 1) / kb);
     size_t smem = (size_t)kb * g.n_views * sizeof(int32_t);
     if (smem > 48 * 1024) return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "shift-and-add: too many views");
+    LaunchTimer lt(plan->ctx, "saa");
     saa_kernel<<<grid, block, smem, plan->ctx->stream>>>(g.nu, g.nv, g.nz, g.n_views, d_shift, proj, out, kb);
     KV_CHECK_LAUNCH(plan->ctx, "saa_kernel");
     return KV_OK;
 }
 
 kv_status fill_launch(kv_ctx *ctx, float *p, size_t n, float v) {
+    LaunchTimer lt(ctx, "fill");
     fill_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(p, n, v);
     KV_CHECK_LAUNCH(ctx, "fill_kernel");
     return KV_OK;
@@ -175,6 +177,7 @@ kv_status fill_launch(kv_ctx *ctx, float *p, size_t n, float v) {
 
 kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_storage s) {
     int gb = grid_for(ctx, n, 256);
+    LaunchTimer lt(ctx, "to_storage");
     if (s == KV_STORAGE_BF16) to_storage_kernel<__nv_bfloat16><<<gb, 256, 0, ctx->stream>>>(in, (__nv_bfloat16 *)out, n);
     else if (s == KV_STORAGE_F16) to_storage_kernel<__half><<<gb, 256, 0, ctx->stream>>>(in, (__half *)out, n);
     else to_storage_kernel<float><<<gb, 256, 0, ctx->stream>>>(in, (float *)out, n);
@@ -184,6 +187,7 @@ kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_s
 
 kv_status convert_back_launch(kv_ctx *ctx, const void *in, float *out, size_t n, kv_storage s) {
     int gb = grid_for(ctx, n, 256);
+    LaunchTimer lt(ctx, "from_storage");
     if (s == KV_STORAGE_BF16) from_storage_kernel<__nv_bfloat16><<<gb, 256, 0, ctx->stream>>>((const __nv_bfloat16 *)in, out, n);
     else if (s == KV_STORAGE_F16) from_storage_kernel<__half><<<gb, 256, 0, ctx->stream>>>((const __half *)in, out, n);
     else from_storage_kernel<float><<<gb, 256, 0, ctx->stream>>>((const float *)in, out, n);
@@ -198,6 +202,7 @@ kv_status phantom_launch(kv_ctx *ctx, int nx, int ny, int nz, float dx, float dy
     if (smem > 48 * 1024)
         KV_CHECK_CUDA(ctx, cudaFuncSetAttribute(phantom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     size_t total = (size_t)nx * ny * nz;
+    LaunchTimer lt(ctx, "phantom");
     phantom_kernel<<<grid_for(ctx, total, 256), 256, smem, ctx->stream>>>(nx, ny, nz, dx, dy, dz, d_params, n, vol);
     KV_CHECK_LAUNCH(ctx, "phantom_kernel");
     return KV_OK;
@@ -207,8 +212,14 @@ kv_status residual_reduce_launch(kv_ctx *ctx, const float *q, const float *p, si
     const int nblocks = ctx->sm_count > 0 ? ctx->sm_count * 4 : 512;
     double *partials = nullptr;
     KV_CHECK_CUDA(ctx, cudaMallocAsync((void **)&partials, (size_t)nblocks * 3 * sizeof(double), ctx->stream));
-    residual_partials_kernel<<<nblocks, 256, 0, ctx->stream>>>(q, p, n, partials);
-    sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(partials, nblocks, red);
+    {
+        LaunchTimer lt(ctx, "residual_partials");
+        residual_partials_kernel<<<nblocks, 256, 0, ctx->stream>>>(q, p, n, partials);
+    }
+    {
+        LaunchTimer lt(ctx, "sum_partials");
+        sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(partials, nblocks, red);
+    }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(partials, ctx->stream);
     if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "residual reduction: %s", cudaGetErrorString(e));

@@ -260,6 +260,7 @@ kv_status rc_forward_launch(kv_plan *plan, const float *d_src, const float *d_or
     RcGeom G = rcgeom(plan, n_views);
     dim3 block(32, 4), grid((G.nu + 31) / 32, (G.nv + 3) / 4, n_views);
     cudaStream_t st = plan->ctx->stream;
+    LaunchTimer lt(plan->ctx, "rc_fwd");
     switch (mode) {
     case RC_PLAIN: rc_forward_kernel<RC_PLAIN><<<grid, block, 0, st>>>(G, d_src, d_org, vol, meas, out, relax); break;
     case RC_MLEM: rc_forward_kernel<RC_MLEM><<<grid, block, 0, st>>>(G, d_src, d_org, vol, meas, out, relax); break;
@@ -273,6 +274,7 @@ kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol)
     RcGeom G = rcgeom(plan, plan->g.n_views);
     dim3 block(32, 4), grid((G.nx + 31) / 32, (G.ny + 3) / 4, G.nz);
     cudaStream_t st = plan->ctx->stream;
+    LaunchTimer lt(plan->ctx, "rc_back");
     switch (mode) {
     case RC_PLAIN: rc_back_kernel<RC_PLAIN><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol); break;
     case RC_MLEM: rc_back_kernel<RC_MLEM><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol); break;
@@ -290,6 +292,7 @@ kv_status rc_residual_launch(kv_plan *plan, const float *q, const float *p, doub
 
 kv_status rc_ratio_launch(kv_plan *plan, int mode, const float *p, float *q, float relax) {
     const int grid = plan->ctx->sm_count > 0 ? plan->ctx->sm_count * 8 : 1024;
+    LaunchTimer lt(plan->ctx, "rc_ratio");
     rc_ratio_kernel<<<grid, 256, 0, plan->ctx->stream>>>(mode, p, q, plan->nproj, relax);
     KV_CHECK_LAUNCH(plan->ctx, "rc_ratio_kernel");
     return KV_OK;

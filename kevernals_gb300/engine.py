@@ -57,6 +57,20 @@ class Context:
     def sync(self):
         self.check(lib().kv_sync(self._h))
 
+    def set_timing(self, enable: bool):
+        """Brackets every kernel launch with CUDA events (tracing)."""
+        self.check(lib().kv_ctx_set_timing(self._h, int(bool(enable))))
+
+    def read_timing(self):
+        """{kernel name: (launches, total device ms)} since the last read."""
+        buf = C.create_string_buffer(1 << 16)
+        self.check(lib().kv_ctx_timing_read(self._h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             lib().kv_ctx_destroy(self._h)

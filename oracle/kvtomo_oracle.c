@@ -121,9 +121,24 @@ int kvo_rc_ray_hits(const kvo_geom *g, int view, int u, int v) {
     return !rc_float_sup_eq(lo, hi);
 }
 
-/* One ray of the RC forward operator.  `alphas` is scratch of >= 4096 floats. */
-static float rc_forward_ray(const kvo_geom *g, const float *vol, int view, int u, int v,
-                            float *alphas) {
+/* Textbook selection sort, the ordering step the reference uses
+ * (Projector.cu:204-220): O(n^2) compares.  Only used to time the reference's
+ * CPU cost; qsort gives the same sorted values. */
+static void selection_sort(float *a, unsigned n) {
+    for (unsigned i = 0; i + 1 < n; ++i) {
+        unsigned m = i;
+        for (unsigned j = i + 1; j < n; ++j)
+            if (a[j] < a[m]) m = j;
+        float t = a[m];
+        a[m] = a[i];
+        a[i] = t;
+    }
+}
+
+/* One ray of the RC forward operator.  `alphas` is scratch of >= 4096 floats.
+ * ref_sort != 0 orders the list with the reference's selection sort. */
+static float rc_forward_ray_sorted(const kvo_geom *g, const float *vol, int view, int u, int v,
+                                   float *alphas, int ref_sort) {
     const int n[3] = {g->nx, g->ny, g->nz};
     const float tol = 0.000001F;
     float s[3], d[3], half[3];
@@ -176,7 +191,8 @@ static float rc_forward_ray(const kvo_geom *g, const float *vol, int view, int u
         }
         start += (a < 2) ? (unsigned)span + 1u : 0u;
     }
-    qsort(alphas, total, sizeof(float), cmp_float);
+    if (ref_sort) selection_sort(alphas, total);
+    else qsort(alphas, total, sizeof(float), cmp_float);
 
     /* midpoint lookup, Projector.cu:345-371: centre in double, truncation */
     float acc = 0.F, wsum = 0.F;
@@ -194,6 +210,11 @@ static float rc_forward_ray(const kvo_geom *g, const float *vol, int view, int u
         }
     }
     return wsum > tol ? acc / wsum : 0.F;
+}
+
+static float rc_forward_ray(const kvo_geom *g, const float *vol, int view, int u, int v,
+                            float *alphas) {
+    return rc_forward_ray_sorted(g, vol, view, u, v, alphas, 0);
 }
 
 void kvo_rc_forward(const kvo_geom *g, const float *vol, float *proj) {
@@ -227,6 +248,25 @@ void kvo_rc_forward_rays(const kvo_geom *g, const float *vol, const int64_t *ray
             int view = (int)(r / per_view);
             long long rem = r % per_view;
             out[i] = rc_forward_ray(g, vol, view, (int)(rem % g->nu), (int)(rem / g->nu), alphas);
+        }
+        free(alphas);
+    }
+}
+
+/* The same, ordering each ray's list with the reference's selection sort:
+ * the reference's own per-ray cost, for timing its CPU path. */
+void kvo_rc_forward_rays_refcost(const kvo_geom *g, const float *vol, const int64_t *rays, int64_t n,
+                                 float *out) {
+    const long long per_view = (long long)g->nu * g->nv;
+#pragma omp parallel
+    {
+        float *alphas = (float *)malloc(4096 * sizeof(float));
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t i = 0; i < n; ++i) {
+            long long r = rays[i];
+            long long rem = r % per_view;
+            out[i] = rc_forward_ray_sorted(g, vol, (int)(r / per_view), (int)(rem % g->nu),
+                                           (int)(rem / g->nu), alphas, 1);
         }
         free(alphas);
     }
@@ -588,6 +628,23 @@ void kvo_exact_back(const kvo_geom *g, const double *proj, double *vol) {
     for (int t = 0; t < nt; ++t)
         for (size_t j = 0; j < nvox; ++j) vol[j] += priv[(size_t)t * nvox + j];
     free(priv);
+}
+
+/* Transpose restricted to a subset of rays: vol += sum_r values[r] * (row r
+ * of A), scattered with atomic adds (for timing the CPU path on a sample). */
+void kvo_exact_back_rays(const kvo_geom *g, const double *values, const int64_t *rays, int64_t n,
+                         double *vol) {
+    const long long per_view = (long long)g->nu * g->nv;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+        long long r = rays[i];
+        long long rem = r % per_view;
+        exact_ray ray;
+        if (!exact_ray_setup(g, (int)(r / per_view), (int)(rem % g->nu) + 0.5, (int)(rem / g->nu) + 0.5, &ray))
+            continue;
+        const double val = values[i];
+        EXACT_WALK(ray, { _Pragma("omp atomic") vol[vidx] += w_mm * val; });
+    }
 }
 
 /* EXACT MLEM in FP64: x <- x * A^T(relax p / A x) / A^T 1. */

@@ -64,6 +64,8 @@ def lib():
             "kvo_exact_forward": [G, _f64p, _f64p],
             "kvo_exact_forward_rays": [G, _f64p, _i64p, C.c_int64, _f64p],
             "kvo_exact_back": [G, _f64p, _f64p],
+            "kvo_exact_back_rays": [G, _f64p, _i64p, C.c_int64, _f64p],
+            "kvo_rc_forward_rays_refcost": [G, _f32p, _i64p, C.c_int64, _f32p],
             "kvo_exact_ray_lengths": [G, _f64p],
             "kvo_exact_mlem": [G, _f64p, _f64p, C.c_int, C.c_double],
             "kvo_exact_sart": [G, _f64p, _f64p, C.c_int, C.c_double],
@@ -125,6 +127,24 @@ def rc_forward_rays(g, vol, rays):
     out = np.empty(rays.shape[0], np.float32)
     lib().kvo_rc_forward_rays(C.byref(cgeom(g)), _vol(g, vol, np.float32), rays, rays.shape[0], out)
     return out
+
+
+def rc_forward_rays_refcost(g, vol, rays):
+    """RC forward of sampled rays with the reference's selection sort."""
+    rays = np.ascontiguousarray(rays, np.int64)
+    out = np.empty(rays.shape[0], np.float32)
+    lib().kvo_rc_forward_rays_refcost(C.byref(cgeom(g)), _vol(g, vol, np.float32), rays,
+                                      rays.shape[0], out)
+    return out
+
+
+def exact_back_rays(g, values, rays, vol):
+    """Adds the transpose of the sampled rays into vol (float64, in place)."""
+    rays = np.ascontiguousarray(rays, np.int64)
+    values = np.ascontiguousarray(values, np.float64)
+    assert vol.dtype == np.float64 and vol.flags.c_contiguous and vol.size == g.n_voxels
+    lib().kvo_exact_back_rays(C.byref(cgeom(g)), values, rays, rays.shape[0], vol)
+    return vol
 
 
 def rc_back_voxels(g, proj, voxels):
