@@ -184,8 +184,8 @@ extern "C" kv_status kv_ctx_create(int device, kv_ctx **out) {
     return KV_OK;
 }
 
-extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
-    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+namespace {
+void ctx_free(kv_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (const kv_timing_rec &r : ctx->timing_recs) {
@@ -196,6 +196,16 @@ extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
     cudaFree(ctx->d_red);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
+}
+}  // namespace
+
+// Releases the caller's reference; the context lives on until its last plan
+// is destroyed, so destroying a context before its plans is safe.
+extern "C" kv_status kv_ctx_destroy(kv_ctx *ctx) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (ctx->released) return kv_fail(ctx, KV_ERR_INVALID_ARG, "context destroyed twice");
+    ctx->released = true;
+    if (ctx->plans == 0) ctx_free(ctx);
     return KV_OK;
 }
 
@@ -308,6 +318,7 @@ extern "C" kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *g, kv_family
     kv_plan *plan = new (std::nothrow) kv_plan;
     if (plan == nullptr) return KV_ERR_OOM;
     plan->ctx = ctx;
+    ctx->plans += 1;
     plan->g = *g;
     plan->src.assign(g->src, g->src + 3 * g->n_views);
     plan->det.assign(g->det_origin, g->det_origin + 3 * g->n_views);
@@ -352,7 +363,9 @@ extern "C" kv_status kv_plan_destroy(kv_plan *plan) {
     cudaFree(plan->d_proj32);
     cudaFree(plan->d_sens);
     cudaFree(plan->d_shift);
+    kv_ctx *ctx = plan->ctx;
     delete plan;
+    if (--ctx->plans == 0 && ctx->released) ctx_free(ctx);
     return KV_OK;
 }
 

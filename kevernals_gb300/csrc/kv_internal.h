@@ -28,6 +28,10 @@ struct kv_ctx {
     cudaStream_t own_stream = nullptr;
     std::string last_error;
     double *d_red = nullptr;         // 8 doubles for FP64 reductions
+    // lifetime: plans hold a reference; kv_ctx_destroy only releases the
+    // caller's, the context is freed with its last plan
+    int plans = 0;
+    bool released = false;
     // per-kernel tracing (kv_ctx_set_timing)
     bool timing = false;
     std::vector<kv_timing_rec> timing_recs;

@@ -8,7 +8,10 @@ torch stream).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import sys
+import weakref
 
 import numpy as np
 
@@ -19,6 +22,21 @@ try:  # torch is optional: only needed for device-resident buffers
     import torch
 except Exception:  # pragma: no cover
     torch = None
+
+
+_LIVE = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    """Destroys every live plan, then every context, before interpreter
+    teardown (a plan must not outlive the CUDA runtime)."""
+    objs = list(_LIVE)
+    for o in objs:
+        if isinstance(o, Plan):
+            o.close()
+    for o in objs:
+        o.close()
 
 
 def _is_cuda_tensor(x):
@@ -35,6 +53,7 @@ class Context:
             raise KvError(s, lib().kv_status_string(s).decode())
         self._h = h
         self.device = device
+        _LIVE.add(self)
 
     @property
     def handle(self):
@@ -77,6 +96,8 @@ class Context:
             self._h = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -107,6 +128,7 @@ class Plan:
                                  _lib.STORAGE[storage], C.byref(h))
         ctx.check(s)
         self._h = h
+        _LIVE.add(self)
 
     @property
     def handle(self):
@@ -118,6 +140,8 @@ class Plan:
             self._h = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
