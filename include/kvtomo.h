@@ -174,6 +174,25 @@ kv_status kv_sart(kv_plan *plan, const float *projections, float *volume_inout, 
 kv_status kv_residual(kv_plan *plan, const float *projections, const float *volume, kv_mem mem,
                       double *rel_residual, double *loglik);
 
+/* The same FP64 residual and log-likelihood as kv_residual, computed without
+ * allocating any device memory.  No reference counterpart.  For callers that
+ * may not allocate when they need a residual: real-time loops that must not
+ * touch the allocator, or hosts whose device memory is owned by another
+ * framework's allocator or a fixed budget.  The plan (created beforehand) must
+ * be KV_FAMILY_EXACT with KV_STORAGE_F32; `projections` and `volume` are
+ * device pointers; the results are written to the two host doubles.
+ * Scratch: a static device array of KV_NOALLOC_MAX_BLOCKS FP64 partial-sum
+ * triples (1.5 MiB) that every GPU loading the library holds until the
+ * process exits; a geometry whose forward projection needs more blocks than
+ * that (ceil(nu/32) * ceil(nv/4) * n_views > KV_NOALLOC_MAX_BLOCKS) is
+ * rejected with KV_ERR_INVALID_ARG -- use kv_residual for it.  The first call
+ * on a device looks up the array's device address, so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on one GPU race and must be serialised by the caller. */
+#define KV_NOALLOC_MAX_BLOCKS 65536
+kv_status kv_residual_noalloc(kv_plan *plan, const float *projections, const float *volume,
+                              double *rel_residual, double *loglik);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,8 @@ SIGNATURES = {
     "kv_sart": ([_vp, _vp, _vp, C.c_int, C.c_float, C.c_int, ITER_CB, _vp], C.c_int),
     "kv_residual": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)],
                     C.c_int),
+    "kv_residual_noalloc": ([_vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+                            C.c_int),
 }
 
 _lib = None

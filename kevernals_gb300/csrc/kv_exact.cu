@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace {
 
@@ -514,5 +515,77 @@ kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(ls, st);
     if (e != cudaSuccess) return kv_fail(plan->ctx, KV_ERR_CUDA, "sensitivity launch: %s", cudaGetErrorString(e));
+    return KV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Residual without device allocation
+// ---------------------------------------------------------------------------
+// kv_residual allocates its per-block partial sums for every call.  Callers
+// that may not allocate device memory when they need a residual -- real-time
+// loops that must not touch the allocator, or hosts whose device memory is
+// owned by another framework's allocator or a fixed budget -- use
+// kv_residual_noalloc instead.  Its scratch is this file-scope array: one FP64
+// triple per forward block (at most KV_NOALLOC_MAX_BLOCKS blocks) and the
+// final three sums, 1.5 MiB that every GPU loading the library holds until
+// the process exits.  Every call overwrites the partials it reads, so nothing
+// has to be cleared between calls; calls that overlap on one GPU share the
+// array and race.
+static __device__ __align__(256) double g_noalloc_scratch[3 * KV_NOALLOC_MAX_BLOCKS + 4];
+
+namespace {
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[64] = {};   // device address of g_noalloc_scratch, per device ordinal
+
+// Set-up, once per device, with that device current: the host-side name of a
+// __device__ array is not a device address; ask the runtime for it.
+kv_status noalloc_scratch(kv_ctx *ctx, double **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    const int dev = ctx->device;
+    if (dev < 0 || dev >= 64) return kv_fail(ctx, KV_ERR_INVALID_ARG, "device ordinal %d out of range", dev);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return kv_fail(ctx, KV_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return KV_OK;
+}
+}  // namespace
+
+extern "C" kv_status kv_residual_noalloc(kv_plan *plan, const float *projections, const float *volume,
+                                         double *rel_residual, double *loglik) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    kv_ctx *ctx = plan->ctx;
+    if (projections == nullptr || volume == nullptr)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_residual_noalloc: null device buffer");
+    if (plan->family != KV_FAMILY_EXACT || plan->storage != KV_STORAGE_F32)
+        return kv_fail(ctx, KV_ERR_UNSUPPORTED, "kv_residual_noalloc: EXACT family with FP32 storage only");
+    const int by = plan->fwd_by;
+    if (by < 1 || by > 8) return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad forward block");
+    const size_t nblocks = (size_t)((plan->g.nu + 31) / 32) * ((plan->g.nv + by - 1) / by) * plan->g.n_views;
+    if (nblocks > KV_NOALLOC_MAX_BLOCKS)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG,
+                       "kv_residual_noalloc: this geometry needs %zu partial sums but the static scratch holds "
+                       "%d (at most %d forward blocks of 32 x %d rays); use kv_residual",
+                       nblocks, KV_NOALLOC_MAX_BLOCKS, KV_NOALLOC_MAX_BLOCKS, by);
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    double *scratch = nullptr;
+    KV_TRY(noalloc_scratch(ctx, &scratch));
+    double *partials = scratch, *sums = scratch + 3 * (size_t)KV_NOALLOC_MAX_BLOCKS;
+    ExGeom G = exgeom(plan, plan->g.n_views);
+    dim3 block(32, by), grid((G.nu + 31) / 32, (G.nv + by - 1) / by, G.n_views);
+    FwdArgs a{volume, projections, nullptr, nullptr, 1.f};
+    exact_fwd_kernel<float, float, FWD_RESID><<<grid, block, 0, ctx->stream>>>(G, plan->ex, a, partials);
+    KV_CHECK_LAUNCH(ctx, "exact_fwd_kernel (no-alloc residual)");
+    reduce_partials_kernel<<<1, 1024, 0, ctx->stream>>>(partials, nblocks, sums);
+    KV_CHECK_LAUNCH(ctx, "reduce_partials_kernel (no-alloc residual)");
+    double h[3];
+    KV_CHECK_CUDA(ctx, cudaMemcpyAsync(h, sums, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (rel_residual) *rel_residual = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+    if (loglik) *loglik = h[2];
     return KV_OK;
 }
