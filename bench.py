@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--views", type=int, default=0,
+                    help="keep only the first N views (smaller case for profiling captures)")
     return ap.parse_args()
 
 
@@ -356,6 +358,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     g, n_ell, i0, cfg, desc = geometry(args.workload)
+    if args.views > 0:
+        g = g.subset_views(np.arange(min(args.views, g.n_views)))
+        desc += f" (first {g.n_views} views only)"
     if args.impl == "reference":
         if rank == 0:
             reference_arm(args, g, desc)
