@@ -169,6 +169,50 @@ kv_status kv_mlem(kv_plan *plan, const float *projections, float *volume_inout, 
  * SART, x <- x + relax * C A^T(R (p - A x)), R = 1/(A 1), C = 1/(A^T 1). */
 kv_status kv_sart(kv_plan *plan, const float *projections, float *volume_inout, int iterations,
                   float relax, kv_mem mem, kv_iter_cb cb, void *user);
+/* Batched MLEM: n independent EXACT/FP32 reconstructions of uneven volume,
+ * detector and view counts, all created on `ctx`, run together.  Each
+ * iteration is one persistent forward launch and one persistent
+ * backprojection launch over the tiles of every problem; the whole
+ * `iterations` loop is captured as one CUDA graph.  Results are identical to
+ * calling kv_mlem on each plan.  No reference counterpart (the reference
+ * reconstructs one case per call).  projections[i] / volumes[i] are host or
+ * device buffers according to `mem`; volumes are updated in place. */
+kv_status kv_batch_mlem(kv_ctx *ctx, int n, kv_plan *const *plans, const float *const *projections,
+                        float *const *volumes, int iterations, float relax, kv_mem mem);
+
+/* Autotuner (no reference counterpart; the reference launches every kernel
+ * with a fixed 32x16 block).  Times the EXACT forward projector with ray
+ * bundles of 32 x {1,2,4,8} and the backprojector with voxel tiles of
+ * 32 x {2,4,8} on (a subset of the views of) this plan's geometry and keeps
+ * the fastest; results are cached per geometry shape for the process. */
+kv_status kv_plan_autotune(kv_plan *plan);
+kv_status kv_plan_get_tuning(const kv_plan *plan, int *fwd_rows, int *back_rows);
+kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_rows);
+
+/* ---- learned warm start (no reference counterpart) ----------------------
+ * A 3D U-Net (4 levels, 16/32/64/128 channels, 3x3x3 convolutions, BF16
+ * weights and activations, FP32 accumulation, tensor-core implicit-GEMM
+ * convolutions) mapping a shift-and-add volume [D][H][W] (float32) to an MLEM
+ * initial estimate of the same size: y = x + f(x).  D and H must be multiples
+ * of 8 and W of 128. */
+typedef struct kv_unet kv_unet;
+kv_status kv_unet_create(kv_ctx *ctx, uint64_t seed, kv_unet **out);
+kv_status kv_unet_destroy(kv_unet *net);
+size_t kv_unet_num_params(const kv_unet *net);
+kv_status kv_unet_forward(kv_unet *net, const float *in, float *out, int32_t D, int32_t H, int32_t W,
+                          kv_mem mem);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the mean squared error
+ * between net(in) and target; *loss is the loss before the step. */
+kv_status kv_unet_train_step(kv_unet *net, const float *in, const float *target, int32_t D, int32_t H,
+                             int32_t W, float lr, float *loss, kv_mem mem);
+/* Loss and FP32 parameter gradients (host buffer of kv_unet_num_params). */
+kv_status kv_unet_gradients(kv_unet *net, const float *in, const float *target, int32_t D, int32_t H,
+                            int32_t W, float *loss, float *grads, kv_mem mem);
+/* Checkpoint state: parameters, Adam moments (3 * num_params host floats) and
+ * the step count. */
+kv_status kv_unet_get_state(const kv_unet *net, float *state, int64_t *step);
+kv_status kv_unet_set_state(kv_unet *net, const float *state, int64_t step);
+
 /* ||A x - p||_2 / ||p||_2 and sum(p log(Ax) - Ax) reduced in FP64.  No
  * reference counterpart (the reference has no stopping criterion). */
 kv_status kv_residual(kv_plan *plan, const float *projections, const float *volume, kv_mem mem,

@@ -61,6 +61,21 @@ SIGNATURES = {
     "kv_sart": ([_vp, _vp, _vp, C.c_int, C.c_float, C.c_int, ITER_CB, _vp], C.c_int),
     "kv_residual": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)],
                     C.c_int),
+    "kv_batch_mlem": ([_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.c_int,
+                       C.c_float, C.c_int], C.c_int),
+    "kv_plan_autotune": ([_vp], C.c_int),
+    "kv_plan_get_tuning": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+    "kv_plan_set_tuning": ([_vp, C.c_int, C.c_int], C.c_int),
+    "kv_unet_create": ([_vp, C.c_uint64, C.POINTER(_vp)], C.c_int),
+    "kv_unet_destroy": ([_vp], C.c_int),
+    "kv_unet_num_params": ([_vp], C.c_size_t),
+    "kv_unet_forward": ([_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_int], C.c_int),
+    "kv_unet_train_step": ([_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                            C.POINTER(C.c_float), C.c_int], C.c_int),
+    "kv_unet_gradients": ([_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_float),
+                           _vp, C.c_int], C.c_int),
+    "kv_unet_get_state": ([_vp, _vp, C.POINTER(C.c_int64)], C.c_int),
+    "kv_unet_set_state": ([_vp, _vp, C.c_int64], C.c_int),
     "kv_residual_noalloc": ([_vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_double)],
                             C.c_int),
 }

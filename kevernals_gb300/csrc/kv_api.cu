@@ -363,10 +363,15 @@ extern "C" kv_status kv_plan_destroy(kv_plan *plan) {
     cudaFree(plan->d_proj32);
     cudaFree(plan->d_sens);
     cudaFree(plan->d_shift);
+    if (plan->graph_exec) cudaGraphExecDestroy(plan->graph_exec);
     kv_ctx *ctx = plan->ctx;
     delete plan;
-    if (--ctx->plans == 0 && ctx->released) ctx_free(ctx);
+    kv_ctx_release_ref(ctx);
     return KV_OK;
+}
+
+void kv_ctx_release_ref(kv_ctx *ctx) {
+    if (--ctx->plans == 0 && ctx->released) ctx_free(ctx);
 }
 
 extern "C" size_t kv_plan_volume_elems(const kv_plan *plan) { return plan ? plan->nvox : 0; }
@@ -537,11 +542,63 @@ namespace {
 // MLEM (mlem = true) or SART/ART (mlem = false) on device buffers: p, x are
 // float32 (RC or F32 storage) or storage-typed (EXACT mixed precision).
 kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax, bool mlem,
+                  kv_iter_cb cb, void *user);
+
+// Without a callback (and without tracing) the iteration loop is captured once
+// as a CUDA graph on the context's own stream and launched on the call's
+// stream; the executable graph is kept and relaunched while the buffers and
+// parameters stay the same.
+kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float relax, bool mlem) {
+    kv_ctx *ctx = plan->ctx;
+    const bool same = plan->graph_exec != nullptr && plan->graph_p == p && plan->graph_x == x &&
+                      plan->graph_iters == iters && plan->graph_mlem == (int)mlem && plan->graph_relax == relax &&
+                      plan->graph_fb == plan->fwd_by && plan->graph_bb == plan->back_by;
+    if (!same) {
+        if (plan->graph_exec != nullptr) {
+            KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            cudaGraphExecDestroy(plan->graph_exec);
+            plan->graph_exec = nullptr;
+        }
+        cudaStream_t user_stream = ctx->stream;
+        ctx->stream = ctx->own_stream;
+        KV_CHECK_CUDA(ctx, cudaStreamBeginCapture(ctx->own_stream, cudaStreamCaptureModeThreadLocal));
+        kv_status s = iterate(plan, p, x, iters, relax, mlem, nullptr, nullptr);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->own_stream, &graph);
+        ctx->stream = user_stream;
+        if (s != KV_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return s;
+        }
+        if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "iteration capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&plan->graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            plan->graph_exec = nullptr;
+            return kv_fail(ctx, KV_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+        plan->graph_p = p;
+        plan->graph_x = x;
+        plan->graph_iters = iters;
+        plan->graph_mlem = (int)mlem;
+        plan->graph_relax = relax;
+        plan->graph_fb = plan->fwd_by;
+        plan->graph_bb = plan->back_by;
+    }
+    KV_CHECK_CUDA(ctx, cudaGraphLaunch(plan->graph_exec, ctx->stream));
+    return KV_OK;
+}
+
+kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax, bool mlem,
                   kv_iter_cb cb, void *user) {
     kv_ctx *ctx = plan->ctx;
     const size_t es = kv_storage_bytes(plan->storage);
     KV_TRY(ensure(ctx, &plan->d_ratio, plan->nproj * es));
     if (plan->family == KV_FAMILY_EXACT) KV_TRY(ensure_sens(plan));
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &cs);
+    if (cb == nullptr && !ctx->timing && iters >= 2 && cs == cudaStreamCaptureStatusNone)
+        return iterate_graph(plan, p, x, iters, relax, mlem);
     for (int it = 0; it < iters; ++it) {
         if (plan->family == KV_FAMILY_EXACT) {
             FwdArgs fa{x, p, plan->d_ratio, cb ? ctx->d_red : nullptr, relax};
@@ -631,4 +688,67 @@ extern "C" kv_status kv_residual(kv_plan *plan, const float *proj, const float *
         KV_TRY(rc_residual_launch(plan, (const float *)plan->d_ratio, pd, plan->ctx->d_red));
     }
     return residual_from_red(plan->ctx, rel_residual, loglik);
+}
+
+// ---------------------------------------------------------------------------
+// Batched solves and tuning
+// ---------------------------------------------------------------------------
+
+extern "C" kv_status kv_batch_mlem(kv_ctx *ctx, int n, kv_plan *const *plans, const float *const *projections,
+                                   float *const *volumes, int iterations, float relax, kv_mem mem) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (n <= 0 || plans == nullptr || projections == nullptr || volumes == nullptr)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_batch_mlem: empty batch or null arrays");
+    if (iterations < 0) return kv_fail(ctx, KV_ERR_INVALID_ARG, "negative iteration count");
+    if (!std::isfinite(relax)) return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite relaxation");
+    if (mem != KV_MEM_HOST && mem != KV_MEM_DEVICE) return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad kv_mem");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    for (int i = 0; i < n; ++i) {
+        kv_plan *pl = plans[i];
+        if (pl == nullptr || projections[i] == nullptr || volumes[i] == nullptr)
+            return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_batch_mlem: null plan or buffer %d", i);
+        if (pl->ctx != ctx) return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_batch_mlem: plan %d has another context", i);
+        if (pl->family != KV_FAMILY_EXACT || pl->storage != KV_STORAGE_F32)
+            return kv_fail(ctx, KV_ERR_UNSUPPORTED, "kv_batch_mlem: EXACT / FP32 plans only (plan %d)", i);
+    }
+    const int by = plans[0]->fwd_by, bb = plans[0]->back_by;
+    std::vector<const float *> pd(n);
+    std::vector<float *> xd(n);
+    for (int i = 0; i < n; ++i) {
+        kv_plan *pl = plans[i];
+        KV_TRY(ensure(ctx, &pl->d_ratio, pl->nproj * sizeof(float)));
+        KV_TRY(ensure_sens(pl));
+        float *a, *b;
+        KV_TRY(stage_in(pl, projections[i], mem, &pl->d_proj32, pl->nproj, true, &a));
+        KV_TRY(stage_in(pl, volumes[i], mem, &pl->d_vol32, pl->nvox, true, &b));
+        pd[i] = a;
+        xd[i] = b;
+    }
+    if (iterations > 0) KV_TRY(exact_batch_mlem_launch(ctx, n, plans, pd.data(), xd.data(), iterations, relax, by, bb));
+    for (int i = 0; i < n; ++i) KV_TRY(stage_out(plans[i], volumes[i], mem, xd[i], plans[i]->nvox));
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_autotune(kv_plan *plan) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (plan->family != KV_FAMILY_EXACT)
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "the autotuner covers the EXACT kernels");
+    KV_CHECK_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+    return exact_autotune(plan);
+}
+
+extern "C" kv_status kv_plan_get_tuning(const kv_plan *plan, int *fwd_rows, int *back_rows) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (fwd_rows) *fwd_rows = plan->fwd_by;
+    if (back_rows) *back_rows = plan->back_by;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_rows) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (fwd_rows < 1 || fwd_rows > 8 || back_rows < 1 || back_rows > 8)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "tuning out of range (1..8 rows of 32 threads)");
+    plan->fwd_by = fwd_rows;
+    plan->back_by = back_rows;
+    return KV_OK;
 }

@@ -55,12 +55,14 @@ __device__ __forceinline__ void lateral_slices(float pos0, float slope, int n, i
     khi = fmaxf(a, b);
 }
 
+// One tile of 32 x blockDim.y rays of view p (tile coordinates bx, by) --
+// the body of the forward kernel, shared by the per-plan launch and the
+// batched persistent kernel.  blin: linear tile index for the partial sums.
 template <typename VolT, typename ProjT, int MODE>
-__global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T, FwdArgs a,
-                                                        double *partials) {
-    const int u = blockIdx.x * 32 + threadIdx.x;
-    const int v = blockIdx.y * blockDim.y + threadIdx.y;
-    const int p = blockIdx.z;
+__device__ __forceinline__ void fwd_tile(const ExGeom &G, const ExactTables &T, const FwdArgs &a,
+                                         double *partials, int bx, int by, int p, size_t blin) {
+    const int u = bx * 32 + threadIdx.x;
+    const int v = by * blockDim.y + threadIdx.y;
     const bool live = (u < G.nu) && (v < G.nv);
     float acc = 0.f, wsum = 0.f, q = 0.f, pm = 0.f;
     size_t ray = 0;
@@ -86,35 +88,117 @@ __global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T,
             k0 = max(0, (int)floorf(klo) - 1);
             k1 = min(G.nz - 1, (int)ceilf(khi) + 1);
         }
+        // interior slices: the whole path in the slice stays two voxels away
+        // from the lateral faces, so no voxel it visits needs a bounds check
+        float ixl, ixh, iyl, iyh;
+        lateral_slices((float)ib + fmaf(X.y, hr0, X.x) - 2.f, X.y * dh, G.nx - 4, G.nz, ixl, ixh);
+        lateral_slices((float)jb + fmaf(Y.y, hr0, Y.x) - 2.f, Y.y * dh, G.ny - 4, G.nz, iyl, iyh);
+        const float kil = fmaxf(fmaxf(ixl, iyl), -2.f), kih = fminf(fminf(ixh, iyh), (float)G.nz + 2.f);
+        int ki0 = (int)ceilf(kil), ki1 = (int)floorf(kih) - 1;   // slice k needs planes k, k+1 inside
+        if (G.nx < 5 || G.ny < 5) {   // no interior: the margins above would invert
+            ki0 = 1;
+            ki1 = 0;
+        }
+
         const VolT *vol = static_cast<const VolT *>(a.vol);
         const size_t plane = (size_t)G.nx * G.ny;
+        const float fmvx = (float)mvx, fmvy = (float)mvy;
+        const int step_y = mvy * G.nx;
         for (int k = k1; k >= k0; --k) {
             const float htop = hr[k + 1];
             const float ftx = __fmaf_rn(X.y, htop, X.x);
             const float fty = __fmaf_rn(Y.y, htop, Y.x);
-            int i = mvx > 0 ? (int)floorf(ftx) : (int)ceilf(ftx) - 1;
-            int j = mvy > 0 ? (int)floorf(fty) : (int)ceilf(fty) - 1;
-            float tx = cross_t(i + ex, ftx, X.z);
-            float ty = cross_t(j + ey, fty, Y.z);
+            const int i = mvx > 0 ? (int)floorf(ftx) : (int)ceilf(ftx) - 1;
+            const int j = mvy > 0 ? (int)floorf(fty) : (int)ceilf(fty) - 1;
+            // next x / y plane as floats (exact integers): cross_t without conversions
+            float fxp = (float)(i + ex), fyp = (float)(j + ey);
+            float tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
+            float ty = __fmul_rn(__fsub_rn(fyp, fty), Y.z);
             float t = 0.f;
             const VolT *slice = vol + (size_t)k * plane;
-            while (true) {
-                const float te = fminf(fminf(tx, ty), 1.0f);
-                const int ai = ib + i, aj = jb + j;
-                if ((unsigned)ai < (unsigned)G.nx && (unsigned)aj < (unsigned)G.ny) {
+            if (k >= ki0 && k <= ki1) {
+                // Row segments of the (warp-uniform) y walk; inside each, the
+                // lane's x crossings.  Weights: same expressions as the
+                // backprojector's min(1, tx_hi, ty_hi) - max(0, tx_lo, ty_lo).
+                // Software-pipelined: the two voxels a row segment can touch
+                // (current column and the next one) are loaded one row ahead.
+                const VolT *ptr = slice + (size_t)(jb + j) * G.nx + (ib + i);
+                float cur0 = Store<VolT>::ld(ptr), cur1 = Store<VolT>::ld(ptr + mvx);
+                while (true) {
+                    const float tb = fminf(ty, 1.0f);
+                    const bool cross = tx < tb;
+                    const VolT *nptr = ptr + (cross ? mvx : 0) + step_y;   // first voxel of the next row
+                    float nxt0 = 0.f, nxt1 = 0.f;
+                    if (tb < 1.0f) {
+                        nxt0 = Store<VolT>::ld(nptr);
+                        nxt1 = Store<VolT>::ld(nptr + mvx);
+                    }
+                    // first piece of the row segment, in the current column
+                    const float te = fminf(tx, tb);
                     const float w = __fsub_rn(te, t);
-                    acc = fmaf(w, Store<VolT>::ld(slice + (size_t)aj * G.nx + ai), acc);
+                    acc = fmaf(w, cur0, acc);
                     if (MODE == FWD_SART) wsum += w;
+                    t = te;
+                    if (cross) {
+                        // the lane crosses a column inside this row segment
+                        ptr += mvx;
+                        fxp += fmvx;
+                        tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
+                        float cv = cur1;
+                        while (tx < tb) {   // rarely: a second crossing in the same row
+                            const float w2 = __fsub_rn(tx, t);
+                            acc = fmaf(w2, cv, acc);
+                            if (MODE == FWD_SART) wsum += w2;
+                            t = tx;
+                            ptr += mvx;
+                            fxp += fmvx;
+                            tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
+                            cv = Store<VolT>::ld(ptr);
+                        }
+                        const float w3 = __fsub_rn(tb, t);
+                        acc = fmaf(w3, cv, acc);
+                        if (MODE == FWD_SART) wsum += w3;
+                        t = tb;
+                        if (tb < 1.0f && ptr + step_y != nptr) {   // after a second crossing
+                            nxt0 = Store<VolT>::ld(ptr + step_y);
+                            nxt1 = Store<VolT>::ld(ptr + step_y + mvx);
+                        }
+                    }
+                    if (tb >= 1.0f) break;
+                    ptr += step_y;
+                    fyp += fmvy;
+                    ty = __fmul_rn(__fsub_rn(fyp, fty), Y.z);
+                    cur0 = nxt0;
+                    cur1 = nxt1;
                 }
-                if (te >= 1.0f) break;
-                if (tx <= ty) {
-                    i += mvx;
-                    tx = cross_t(i + ex, ftx, X.z);
-                } else {
-                    j += mvy;
-                    ty = cross_t(j + ey, fty, Y.z);
+            } else {
+                int ai = ib + i, aj = jb + j;
+                while (true) {
+                    const float tb = fminf(ty, 1.0f);
+                    const bool row_in = (unsigned)aj < (unsigned)G.ny;
+                    const VolT *row = slice + (size_t)(row_in ? aj : 0) * G.nx;
+                    while (tx < tb) {
+                        if (row_in && (unsigned)ai < (unsigned)G.nx) {
+                            const float w = __fsub_rn(tx, t);
+                            acc = fmaf(w, Store<VolT>::ld(row + ai), acc);
+                            if (MODE == FWD_SART) wsum += w;
+                        }
+                        t = tx;
+                        ai += mvx;
+                        fxp += fmvx;
+                        tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
+                    }
+                    if (row_in && (unsigned)ai < (unsigned)G.nx) {
+                        const float w = __fsub_rn(tb, t);
+                        acc = fmaf(w, Store<VolT>::ld(row + ai), acc);
+                        if (MODE == FWD_SART) wsum += w;
+                    }
+                    t = tb;
+                    if (tb >= 1.0f) break;
+                    aj += mvy;
+                    fyp += fmvy;
+                    ty = __fmul_rn(__fsub_rn(fyp, fty), Y.z);
                 }
-                t = te;
             }
         }
         const float ls = ray_factor(X.w, Y.w, VI);
@@ -161,13 +245,19 @@ __global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T,
                 d2 += __shfl_xor_sync(0xffffffffu, d2, o);
             }
             if (threadIdx.x == 0) {
-                const size_t b = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-                partials[3 * b + 0] = d0;
-                partials[3 * b + 1] = d1;
-                partials[3 * b + 2] = d2;
+                partials[3 * blin + 0] = d0;
+                partials[3 * blin + 1] = d1;
+                partials[3 * blin + 2] = d2;
             }
         }
     }
+}
+
+template <typename VolT, typename ProjT, int MODE>
+__global__ void __launch_bounds__(256) exact_fwd_kernel(ExGeom G, ExactTables T, FwdArgs a,
+                                                        double *partials) {
+    fwd_tile<VolT, ProjT, MODE>(G, T, a, partials, blockIdx.x, blockIdx.y, blockIdx.z,
+                                ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 // Sums the per-block partials into out[0..2] (single block).
@@ -214,18 +304,27 @@ __global__ void prescale_kernel(ExGeom G, ExactTables T, const float *y, ProjT *
 // warp w owns row j.  For every view, each warp computes the slice-local
 // y-intervals of its candidate detector rows once into shared memory; each
 // lane then loops over the candidate columns u of its voxel.
-template <typename VolT, typename ProjT, typename AccT, int MODE, bool KAHAN>
-__global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T, BackArgs a,
-                                                         double *sens_out) {
+// Accumulators of the backprojector: plain FP32, Kahan-compensated FP32 (the
+// reduced-precision storage modes), and a double-float sum of exact products
+// (TwoProduct + TwoSum in FP32 arithmetic, ~1e-14 relative) for the FP64
+// sensitivity image.
+enum { ACC_F32 = 0, ACC_KAHAN = 1, ACC_DF = 2 };
+
+// Candidate detector columns a lane holds in registers at once (a voxel at
+// the chest-DT geometry has 4-7).
+constexpr int BACK_SLOTS = 8;
+
+template <typename VolT, typename ProjT, int ACC, int MODE>
+__device__ __forceinline__ void back_tile(const ExGeom &G, const ExactTables &T, const BackArgs &a,
+                                          double *sens_out, int bx, int by, int k) {
     const int lane = threadIdx.x, warp = threadIdx.y;
-    const int i = blockIdx.x * 32 + lane;
-    const int j = blockIdx.y * blockDim.y + warp;
-    const int k = blockIdx.z;
+    const int i = bx * 32 + lane;
+    const int j = by * blockDim.y + warp;
     __shared__ float2 ysh[16][32];
     const bool live_i = i < G.nx;
     const bool live_j = j < G.ny;   // warp-uniform
     const ProjT *yp = static_cast<const ProjT *>(a.yp);
-    AccT acc = 0, comp = 0;
+    float acc = 0.f, comp = 0.f;
     if (live_j) {
         for (int p = 0; p < G.n_views; ++p) {
             const float *hr = T.hr + (size_t)p * (G.nz + 1);
@@ -254,26 +353,56 @@ __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T
                 }
                 __syncwarp();
                 const int nvc = min(32, v1 - vb + 1);
-                for (int u = u0; u <= u1; ++u) {
-                    const float4 X = T.xt[(size_t)p * G.nu + u];
-                    const int ib = T.xi[(size_t)p * G.nu + u];
-                    const float ftx = __fmaf_rn(X.y, htop, X.x);
-                    const float ta = cross_t(i - ib, ftx, X.z), tb = cross_t(i + 1 - ib, ftx, X.z);
-                    const float lox = fmaxf(0.f, fminf(ta, tb)), hix = fminf(1.f, fmaxf(ta, tb));
-                    if (!(hix > lox)) continue;
-                    const ProjT *col = yp + ((size_t)p * G.nv + vb) * G.nu + u;
-                    for (int c = 0; c < nvc; ++c) {
+                // the lane's candidate columns, up to BACK_SLOTS at a time, with
+                // their x-intervals in registers; empty slots get lo > hi.
+                // The chunk loop runs the same number of times in every lane
+                // (the widest lane's count, taken while the warp is converged),
+                // so slots beyond it are skipped with a warp-uniform branch.
+                const int n_u = u1 >= u0 ? u1 - u0 + 1 : 0;
+                const int n_u_warp = __reduce_max_sync(0xffffffffu, n_u);
+                for (int cb = 0; cb * BACK_SLOTS < n_u_warp; ++cb) {
+                    const int ub = u0 + cb * BACK_SLOTS;
+                    const int nslot = min(BACK_SLOTS, n_u_warp - cb * BACK_SLOTS);
+                    float lox[BACK_SLOTS], hix[BACK_SLOTS];
+#pragma unroll
+                    for (int s = 0; s < BACK_SLOTS; ++s) {
+                        lox[s] = 1.f;
+                        hix[s] = 0.f;
+                        const int u = ub + s;
+                        if (u <= u1) {
+                            const float4 X = T.xt[(size_t)p * G.nu + u];
+                            const int ib = T.xi[(size_t)p * G.nu + u];
+                            const float ftx = __fmaf_rn(X.y, htop, X.x);
+                            const float ta = cross_t(i - ib, ftx, X.z), tb = cross_t(i + 1 - ib, ftx, X.z);
+                            lox[s] = fmaxf(0.f, fminf(ta, tb));
+                            hix[s] = fminf(1.f, fmaxf(ta, tb));
+                        }
+                    }
+                    const ProjT *row = yp + ((size_t)p * G.nv + vb) * G.nu + ub;
+                    for (int c = 0; c < nvc; ++c, row += G.nu) {
                         const float2 yi = ysh[warp][c];
-                        const float w = __fsub_rn(fminf(hix, yi.y), fmaxf(lox, yi.x));
-                        if (w > 0.f) {
-                            const AccT term = (AccT)w * (AccT)Store<ProjT>::ld(col + (size_t)c * G.nu);
-                            if (KAHAN) {  // compensated (Kahan) summation
-                                const AccT y_ = term - comp;
-                                const AccT t_ = acc + y_;
-                                comp = (t_ - acc) - y_;
-                                acc = t_;
-                            } else {
-                                acc += term;
+#pragma unroll
+                        for (int s = 0; s < BACK_SLOTS; ++s) {
+                            if (s >= nslot) break;
+                            const float w = __fsub_rn(fminf(hix[s], yi.y), fmaxf(lox[s], yi.x));
+                            if (w > 0.f) {
+                                const float yv = Store<ProjT>::ld(row + s);
+                                if (ACC == ACC_KAHAN) {         // compensated (Kahan) summation
+                                    const float y_ = __fsub_rn(__fmul_rn(w, yv), comp);
+                                    const float t_ = __fadd_rn(acc, y_);
+                                    comp = __fsub_rn(__fsub_rn(t_, acc), y_);
+                                    acc = t_;
+                                } else if (ACC == ACC_DF) {     // exact product + TwoSum: a double-float sum
+                                    const float pr = __fmul_rn(w, yv);
+                                    const float pe = __fmaf_rn(w, yv, -pr);
+                                    const float s_ = __fadd_rn(acc, pr);
+                                    const float bp = __fsub_rn(s_, acc);
+                                    const float er = __fadd_rn(__fsub_rn(acc, __fsub_rn(s_, bp)), __fsub_rn(pr, bp));
+                                    acc = s_;
+                                    comp = __fadd_rn(comp, __fadd_rn(er, pe));
+                                } else {
+                                    acc = fmaf(w, yv, acc);
+                                }
                             }
                         }
                     }
@@ -285,7 +414,7 @@ __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T
     if (!live_i || !live_j) return;
     const size_t idx = ((size_t)k * G.ny + j) * G.nx + i;
     if (sens_out != nullptr) {
-        sens_out[idx] = (double)acc;
+        sens_out[idx] = ACC == ACC_DF ? (double)acc + (double)comp : (double)acc;
         return;
     }
     VolT *vol = static_cast<VolT *>(a.vol);
@@ -300,6 +429,12 @@ __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T
         if (s > 0.0)
             Store<VolT>::st(vol + idx, Store<VolT>::ld_rw(vol + idx) + (float)((double)(a.relax * b) / s));
     }
+}
+
+template <typename VolT, typename ProjT, int ACC, int MODE>
+__global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T, BackArgs a,
+                                                         double *sens_out) {
+    back_tile<VolT, ProjT, ACC, MODE>(G, T, a, sens_out, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 ExGeom exgeom(const kv_plan *plan, int n_views) {
@@ -427,15 +562,15 @@ kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool ka
     LaunchTimer lt(plan->ctx, "exact_back");
     if (kahan) {
         switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, float, BACK_PLAIN, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, float, BACK_MLEM, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, float, BACK_SART, true><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
         }
     } else {
         switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, float, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, float, BACK_MLEM, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, float, BACK_SART, false><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
         }
     }
     KV_CHECK_LAUNCH(plan->ctx, "exact_back_kernel");
@@ -471,7 +606,7 @@ kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int P, FwdMo
 }
 
 kv_status exact_back_launch(kv_plan *plan, BackMode mode, const BackArgs &a) {
-    if (plan->back_by < 1 || plan->back_by > 16) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad back block");
+    if (plan->back_by < 1 || plan->back_by > 8) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad back block");
     switch (plan->storage) {
     case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, true);
     case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, true);
@@ -510,7 +645,7 @@ kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
     {
         LaunchTimer lt(plan->ctx, "exact_back_sens_f64");
-        exact_back_kernel<float, float, double, BACK_PLAIN, false><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
+        exact_back_kernel<float, float, ACC_DF, BACK_PLAIN><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
     }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(ls, st);
@@ -587,5 +722,254 @@ extern "C" kv_status kv_residual_noalloc(kv_plan *plan, const float *projections
     KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (rel_residual) *rel_residual = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
     if (loglik) *loglik = h[2];
+    return KV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched solves: many EXACT reconstructions of uneven size in one launch
+// ---------------------------------------------------------------------------
+// The forward and the backprojection of every problem are cut into the same
+// tiles the per-plan kernels use.  A persistent kernel (a few CTAs per SM)
+// pulls tile indices from a device counter and finds the problem of each tile
+// by binary search over the problems' first tile indices, then runs the very
+// same tile function: results are bit-identical to solving one by one.
+namespace {
+
+struct BatchItem {
+    ExGeom G;
+    ExactTables T;
+    const float *p;        // measured projections
+    float *x;              // iterate (updated in place)
+    float *ratio;          // forward output: Ls * relax * p / Ax
+    const double *sens;    // A^T 1
+    int ftx, fty;          // forward tiles per view (u, v)
+    int btx, bty;          // backprojection tiles per slice (i, j)
+    long long f0, b0;      // first forward / backprojection tile of this problem
+};
+
+__device__ __forceinline__ int batch_find(const BatchItem *items, int n, long long tile, bool fwd) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const long long start = fwd ? items[mid].f0 : items[mid].b0;
+        if (start <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) batch_fwd_kernel(const BatchItem *__restrict__ items, int n,
+                                                        long long total, unsigned long long *counter,
+                                                        float relax) {
+    __shared__ long long s_tile;
+    while (true) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) s_tile = (long long)atomicAdd(counter, 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        __syncthreads();
+        if (tile >= total) return;
+        const BatchItem &B = items[batch_find(items, n, tile, true)];
+        const long long local = tile - B.f0;
+        const long long per_view = (long long)B.ftx * B.fty;
+        const int p = (int)(local / per_view);
+        const int rem = (int)(local % per_view);
+        FwdArgs a{B.x, B.p, B.ratio, nullptr, relax};
+        fwd_tile<float, float, FWD_MLEM>(B.G, B.T, a, nullptr, rem % B.ftx, rem / B.ftx, p, 0);
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_back_kernel(const BatchItem *__restrict__ items, int n,
+                                                         long long total, unsigned long long *counter,
+                                                         float relax) {
+    __shared__ long long s_tile;
+    while (true) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) s_tile = (long long)atomicAdd(counter, 1ull);
+        __syncthreads();
+        const long long tile = s_tile;
+        __syncthreads();
+        if (tile >= total) return;
+        const BatchItem &B = items[batch_find(items, n, tile, false)];
+        const long long local = tile - B.b0;
+        const long long per_slice = (long long)B.btx * B.bty;
+        const int k = (int)(local / per_slice);
+        const int rem = (int)(local % per_slice);
+        BackArgs a{B.ratio, B.x, B.sens, relax};
+        back_tile<float, float, ACC_F32, BACK_MLEM>(B.G, B.T, a, nullptr, rem % B.btx, rem / B.btx, k);
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+// Captures `iters` MLEM iterations over all problems as one CUDA graph and
+// launches it on the context stream.  Plans must be EXACT / FP32 with their
+// sensitivity images computed and ratio workspaces allocated; p[i] / x[i] are
+// device buffers.  Block shape: 32 x by (forward) and 32 x bb (backprojection).
+kv_status exact_batch_mlem_launch(kv_ctx *ctx, int n, kv_plan *const *plans, const float *const *p,
+                                  float *const *x, int iters, float relax, int by, int bb) {
+    std::vector<BatchItem> items(n);
+    long long f = 0, b = 0;
+    for (int i = 0; i < n; ++i) {
+        const kv_plan *pl = plans[i];
+        BatchItem &it = items[i];
+        it.G = exgeom(pl, pl->g.n_views);
+        it.T = pl->ex;
+        it.p = p[i];
+        it.x = x[i];
+        it.ratio = static_cast<float *>(pl->d_ratio);
+        it.sens = pl->d_sens;
+        it.ftx = (pl->g.nu + 31) / 32;
+        it.fty = (pl->g.nv + by - 1) / by;
+        it.btx = (pl->g.nx + 31) / 32;
+        it.bty = (pl->g.ny + bb - 1) / bb;
+        it.f0 = f;
+        it.b0 = b;
+        f += (long long)it.ftx * it.fty * pl->g.n_views;
+        b += (long long)it.btx * it.bty * pl->g.nz;
+    }
+    cudaStream_t cap = ctx->own_stream;
+    BatchItem *d_items = nullptr;
+    unsigned long long *d_counter = nullptr;
+    KV_CHECK_CUDA(ctx, cudaMalloc((void **)&d_items, n * sizeof(BatchItem)));
+    kv_status s = KV_OK;
+    if (cudaMalloc((void **)&d_counter, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(d_items);
+        return kv_fail(ctx, KV_ERR_OOM, "batch counters");
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int occ_f = 0, occ_b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_fwd_kernel, 32 * by, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, batch_back_kernel, 32 * bb, 0);
+    const int grid_f = ctx->sm_count * (occ_f > 0 ? occ_f : 1);
+    const int grid_b = ctx->sm_count * (occ_b > 0 ? occ_b : 1);
+    do {
+        if (cudaMemcpyAsync(d_items, items.data(), n * sizeof(BatchItem), cudaMemcpyHostToDevice, ctx->stream) !=
+            cudaSuccess) { s = kv_fail(ctx, KV_ERR_CUDA, "batch descriptor upload"); break; }
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) { s = kv_fail(ctx, KV_ERR_CUDA, "batch sync"); break; }
+        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            s = kv_fail(ctx, KV_ERR_CUDA, "batch graph capture");
+            break;
+        }
+        for (int it = 0; it < iters; ++it) {
+            cudaMemsetAsync(d_counter, 0, 2 * sizeof(unsigned long long), cap);
+            batch_fwd_kernel<<<grid_f, dim3(32, by), 0, cap>>>(d_items, n, f, d_counter, relax);
+            batch_back_kernel<<<grid_b, dim3(32, bb), 0, cap>>>(d_items, n, b, d_counter + 1, relax);
+        }
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        if (e != cudaSuccess) { s = kv_fail(ctx, KV_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e)); break; }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e != cudaSuccess) { s = kv_fail(ctx, KV_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); break; }
+        LaunchTimer lt(ctx, "batch_mlem_graph");
+        e = cudaGraphLaunch(exec, ctx->stream);
+        if (e != cudaSuccess) { s = kv_fail(ctx, KV_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e)); break; }
+    } while (0);
+    cudaStreamSynchronize(ctx->stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(d_items);
+    cudaFree(d_counter);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: ray-bundle and voxel-tile shapes
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename VolT, typename ProjT>
+float time_fwd(kv_ctx *ctx, const ExGeom &G, const ExactTables &T, const void *vol, void *out, int by,
+               cudaEvent_t e0, cudaEvent_t e1) {
+    dim3 block(32, by), grid((G.nu + 31) / 32, (G.nv + by - 1) / by, G.n_views);
+    FwdArgs a{vol, nullptr, out, nullptr, 1.f};
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(e0, ctx->stream);
+        exact_fwd_kernel<VolT, ProjT, FWD_PLAIN><<<grid, block, 0, ctx->stream>>>(G, T, a, nullptr);
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    return best;
+}
+
+template <typename VolT, typename ProjT, int ACC>
+float time_back(kv_ctx *ctx, const ExGeom &G, const ExactTables &T, const void *yp, void *vol, int bb,
+                cudaEvent_t e0, cudaEvent_t e1) {
+    dim3 block(32, bb), grid((G.nx + 31) / 32, (G.ny + bb - 1) / bb, G.nz);
+    BackArgs a{yp, vol, nullptr, 1.f};
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(e0, ctx->stream);
+        exact_back_kernel<VolT, ProjT, ACC, BACK_PLAIN><<<grid, block, 0, ctx->stream>>>(G, T, a, nullptr);
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    return best;
+}
+
+template <typename VolT, typename ProjT, int ACC>
+void tune(kv_ctx *ctx, const ExGeom &G, const ExactTables &T, void *vol, void *proj, int &fwd_by, int &back_by) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int by : {1, 2, 4, 8}) {
+        const float ms = time_fwd<VolT, ProjT>(ctx, G, T, vol, proj, by, e0, e1);
+        if (ms < best) { best = ms; fwd_by = by; }
+    }
+    best = 1e30f;
+    for (int bb : {2, 4, 8}) {   // 256 threads per block at most
+        const float ms = time_back<VolT, ProjT, ACC>(ctx, G, T, proj, vol, bb, e0, e1);
+        if (ms < best) { best = ms; back_by = bb; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+}
+
+std::mutex g_tune_mutex;
+std::vector<std::pair<std::vector<long long>, std::pair<int, int>>> g_tune_cache;
+
+}  // namespace
+
+// Times the candidate shapes on the plan's own tables with a subset of its
+// views (at most 6: the cost per view is nearly uniform), on zero-filled
+// buffers (the Siddon walk does not depend on the values).
+kv_status exact_autotune(kv_plan *plan) {
+    kv_ctx *ctx = plan->ctx;
+    const kv_geometry &g = plan->g;
+    const std::vector<long long> key = {g.nx, g.ny, g.nz, g.nu, g.nv, g.n_views, (long long)plan->storage};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        for (const auto &e : g_tune_cache)
+            if (e.first == key) {
+                plan->fwd_by = e.second.first;
+                plan->back_by = e.second.second;
+                return KV_OK;
+            }
+    }
+    const size_t es = kv_storage_bytes(plan->storage);
+    if (plan->d_vol == nullptr) KV_CHECK_CUDA(ctx, cudaMalloc(&plan->d_vol, plan->nvox * es));
+    if (plan->d_ratio == nullptr) KV_CHECK_CUDA(ctx, cudaMalloc(&plan->d_ratio, plan->nproj * es));
+    KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_vol, 0, plan->nvox * es, ctx->stream));
+    KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_ratio, 0, plan->nproj * es, ctx->stream));
+    const ExGeom G = exgeom(plan, g.n_views < 6 ? g.n_views : 6);
+    int fb = plan->fwd_by, bb = plan->back_by;
+    switch (plan->storage) {
+    case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
+    case KV_STORAGE_F16: tune<__half, __half, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
+    default: tune<float, float, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+    plan->fwd_by = fb;
+    plan->back_by = bb;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache.emplace_back(key, std::make_pair(fb, bb));
     return KV_OK;
 }

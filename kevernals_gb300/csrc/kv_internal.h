@@ -96,7 +96,23 @@ struct kv_plan {
     // launch tuning (set by kv_plan_autotune or defaults)
     int fwd_by = 4;                  // forward block = 32 x fwd_by rays
     int back_by = 8;                 // backprojector block = 32 x back_by voxels
+
+    // captured iteration loop (kv_mlem / kv_sart without callback), reused
+    // while the buffers and parameters are the same
+    cudaGraphExec_t graph_exec = nullptr;
+    const void *graph_p = nullptr;
+    const void *graph_x = nullptr;
+    int graph_iters = 0, graph_mlem = 0, graph_fb = 0, graph_bb = 0;
+    float graph_relax = 0.f;
 };
+
+// Drops one reference a plan (or network) held on its context; frees the
+// context when it was destroyed by its owner and this was the last one.
+void kv_ctx_release_ref(kv_ctx *ctx);
+
+kv_status exact_batch_mlem_launch(kv_ctx *ctx, int n, kv_plan *const *plans, const float *const *p,
+                                  float *const *x, int iters, float relax, int by, int bb);
+kv_status exact_autotune(kv_plan *plan);
 
 // ---------------------------------------------------------------------------
 // Errors

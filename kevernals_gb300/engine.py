@@ -292,3 +292,140 @@ def phantom(ctx: Context, geometry, params, device=False):
                                           C.c_void_p(params.ctypes.data), params.shape[0],
                                           C.c_void_p(out.ctypes.data), _lib.MEM_HOST))
     return out
+
+
+def _plan_autotune(self):
+    """Chooses the forward ray-bundle and backprojector tile shapes by timing."""
+    self.ctx.check(lib().kv_plan_autotune(self._h))
+    return self.tuning
+
+
+def _plan_tuning(self):
+    f, b = C.c_int(), C.c_int()
+    self.ctx.check(lib().kv_plan_get_tuning(self._h, C.byref(f), C.byref(b)))
+    return f.value, b.value
+
+
+def _plan_set_tuning(self, fwd_rows, back_rows):
+    self.ctx.check(lib().kv_plan_set_tuning(self._h, int(fwd_rows), int(back_rows)))
+
+
+Plan.autotune = _plan_autotune
+Plan.tuning = property(_plan_tuning)
+Plan.set_tuning = _plan_set_tuning
+
+
+def batch_mlem(ctx: Context, plans, projections, volumes, iterations, relax=1.0):
+    """MLEM on many EXACT plans at once (kv_batch_mlem); volumes updated in place.
+    Buffers are all numpy (host) or all CUDA tensors (device)."""
+    n = len(plans)
+    if not (len(projections) == len(volumes) == n) or n == 0:
+        raise ValueError("one projection stack and one volume per plan")
+    keep, pp, pv, mem = [], [], [], None
+    for plan, p, x in zip(plans, projections, volumes):
+        a, m1, k1 = plan._buf(p, plan.geometry.proj_shape)
+        if not _is_cuda_tensor(x) and not (isinstance(x, np.ndarray) and x.dtype == np.float32
+                                           and x.flags.c_contiguous):
+            raise ValueError("volumes must be C-contiguous float32 (updated in place)")
+        b, m2, k2 = plan._buf(x, plan.geometry.volume_shape, out=True)
+        if mem is None:
+            mem = m1
+        if m1 != mem or m2 != mem:
+            raise ValueError("all buffers must be host or all device")
+        keep += [k1, k2]
+        pp.append(a.value)
+        pv.append(b.value)
+    hp = (C.c_void_p * n)(*[plan.handle.value for plan in plans])
+    ap = (C.c_void_p * n)(*pp)
+    av = (C.c_void_p * n)(*pv)
+    ctx.check(lib().kv_batch_mlem(ctx.handle, n, hp, ap, av, int(iterations), float(relax), mem))
+
+
+class UNet:
+    """The learned warm start (kv_unet): y = x + f(x) on [D][H][W] volumes."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(lib().kv_unet_create(ctx.handle, C.c_uint64(seed), C.byref(h)))
+        self._h = h
+        _LIVE.add(self)
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().kv_unet_num_params(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().kv_unet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _io(self, x, out=False):
+        if _is_cuda_tensor(x):
+            if x.dtype != torch.float32 or not x.is_contiguous():
+                raise ValueError("device volumes must be contiguous float32")
+            self.ctx.use_torch_stream()
+            return C.c_void_p(x.data_ptr()), _lib.MEM_DEVICE, x
+        a = x if out else np.ascontiguousarray(x, np.float32)
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            raise ValueError("host volumes must be C-contiguous float32")
+        return C.c_void_p(a.ctypes.data), _lib.MEM_HOST, a
+
+    def forward(self, x, out=None):
+        D, H, W = x.shape
+        if out is None:
+            out = torch.empty_like(x) if _is_cuda_tensor(x) else np.empty((D, H, W), np.float32)
+        pi, m, k1 = self._io(x)
+        po, m2, k2 = self._io(out, out=True)
+        self.ctx.check(lib().kv_unet_forward(self._h, pi, po, D, H, W, m))
+        return out
+
+    def train_step(self, x, target, lr=1e-3):
+        D, H, W = x.shape
+        pi, m, k1 = self._io(x)
+        pt, m2, k2 = self._io(target)
+        loss = C.c_float()
+        self.ctx.check(lib().kv_unet_train_step(self._h, pi, pt, D, H, W, float(lr), C.byref(loss), m))
+        return loss.value
+
+    def gradients(self, x, target):
+        D, H, W = x.shape
+        pi, m, k1 = self._io(x)
+        pt, m2, k2 = self._io(target)
+        g = np.empty(self.num_params, np.float32)
+        loss = C.c_float()
+        self.ctx.check(lib().kv_unet_gradients(self._h, pi, pt, D, H, W, C.byref(loss),
+                                               C.c_void_p(g.ctypes.data), m))
+        return loss.value, g
+
+    def get_state(self):
+        st = np.empty(3 * self.num_params, np.float32)
+        step = C.c_int64()
+        self.ctx.check(lib().kv_unet_get_state(self._h, C.c_void_p(st.ctypes.data), C.byref(step)))
+        return st, step.value
+
+    def set_state(self, state, step):
+        st = np.ascontiguousarray(state, np.float32)
+        if st.size != 3 * self.num_params:
+            raise ValueError("state size mismatch")
+        self.ctx.check(lib().kv_unet_set_state(self._h, C.c_void_p(st.ctypes.data), int(step)))
+
+    @property
+    def params(self):
+        return self.get_state()[0][: self.num_params]
+
+    def save(self, path):
+        st, step = self.get_state()
+        np.savez(path, state=st, step=step)
+
+    def load(self, path):
+        z = np.load(path)
+        self.set_state(z["state"], int(z["step"]))

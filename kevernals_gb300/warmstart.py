@@ -1,0 +1,203 @@
+"""Learned warm start for MLEM.
+
+Input of the network: the volume-grid shift-and-add,
+    s = A^T (p / A 1) / A^T 1,
+the mean attenuation of the rays through each voxel averaged over the views --
+exactly one SART step from zero (kv_sart, relax 1).  Target: the MLEM iterate
+after `target_iters` iterations from the uniform start.  Training triples
+(phantom, shift-and-add, MLEM target) are generated by the engine itself.
+
+warm_start_mlem() keeps plain MLEM as the judge: the network's estimate is
+used only if its data residual ||A x0 - p|| / ||p|| is no worse than the
+uniform start's; otherwise MLEM starts from the uniform volume.
+
+CLI (writes a checkpoint and a JSON report):
+    python -m kevernals_gb300.warmstart train --out DIR [--triples N] ...
+    python -m kevernals_gb300.warmstart evaluate --ckpt FILE [--cases N] ...
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+from . import engine, phantom as ph
+from .geometry import Geometry, config_chest, linear_sweep
+
+EPS = 1e-4   # MLEM needs a strictly positive start
+
+
+def crop_geometry(nx=256, ny=256, nz=64, n_views=60, half_angle=17.5) -> Geometry:
+    """Training crop at the chest-DT voxel size (0.4 x 0.4 x 2.5 mm) and
+    acquisition (60 views over +-17.5 deg); a 1024^2 detector at 0.2 mm covers
+    the crop and its oblique shadows."""
+    return linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, n_views, 1024, 1024, 0.2, 0.2, half_angle)
+
+
+def noisy_data(ctx, plan, truth, i0, seed):
+    import torch
+    line = plan.forward(truth)
+    gen = torch.Generator(device=line.device).manual_seed(int(seed))
+    counts = torch.poisson(i0 * torch.exp(-line.double()), generator=gen)
+    return torch.log(i0 / counts.clamp_min(1.0)).clamp_min(0.0).float().contiguous()
+
+
+def shift_and_add_volume(plan, p):
+    """A^T(p / A1) / A^T1: one SART step (relax 1) from zero."""
+    import torch
+    x = torch.zeros(plan.geometry.volume_shape, dtype=torch.float32, device=p.device)
+    plan.sart(p, x, 1, 1.0)
+    return x
+
+
+def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100):
+    """(shift-and-add, MLEM target, data) for one seeded phantom, on the GPU."""
+    import torch
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
+    truth = engine.phantom(ctx, g, params, device=True)
+    plan = engine.Plan(ctx, g, "exact")
+    p = noisy_data(ctx, plan, truth, i0, seed)
+    s = shift_and_add_volume(plan, p)
+    x = torch.ones(g.volume_shape, dtype=torch.float32, device=p.device)
+    plan.mlem(p, x, target_iters)
+    torch.cuda.synchronize()
+    plan.close()
+    return s, x, p
+
+
+def train(net, triples, epochs, lr=1e-3, seed=0, log=None):
+    rng = np.random.default_rng(seed)
+    history = []
+    for ep in range(epochs):
+        order = rng.permutation(len(triples))
+        losses = [net.train_step(triples[i][0], triples[i][1], lr) for i in order]
+        history.append(float(np.mean(losses)))
+        if log:
+            log(f"epoch {ep + 1}/{epochs}: mean loss {history[-1]:.4e}")
+    return history
+
+
+def warm_start(plan, net, p):
+    """Initial estimate: the network's, if its data residual is no worse than
+    the uniform start's; returns (x0, accepted, residual_warm, residual_uniform)."""
+    import torch
+    s = shift_and_add_volume(plan, p)
+    x0 = net.forward(s).clamp_(min=EPS)
+    ones = torch.ones_like(x0)
+    r_w, _ = plan.residual(p, x0)
+    r_u, _ = plan.residual(p, ones)
+    if r_w <= r_u:
+        return x0, True, r_w, r_u
+    return ones, False, r_w, r_u
+
+
+def iterations_to_residual(plan, p, x, target, max_iters):
+    """MLEM from x until ||Ax - p|| / ||p|| <= target; returns (iterations, residual)."""
+    state = {"n": max_iters, "r": None}
+
+    def cb(it, res, ll):
+        # res is the residual of the iterate entering iteration `it`, i.e.
+        # after `it` updates; stopping here skips that update
+        state["r"] = res
+        state["n"] = it
+        return res <= target or it >= max_iters
+    plan.mlem(p, x, max_iters + 1, callback=cb)
+    return state["n"], state["r"]
+
+
+def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipsoids=400):
+    """Plain MLEM (uniform start, plain_iters iterations) vs the warm start
+    reaching the same data residual within `tol`: iterations and wall time."""
+    import torch
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
+    truth = engine.phantom(ctx, g, params, device=True)
+    plan = engine.Plan(ctx, g, "exact")
+    p = noisy_data(ctx, plan, truth, i0, seed)
+    plan.sensitivity(device=True)          # one-time per geometry, outside both timings
+    torch.cuda.synchronize()
+    # plain MLEM
+    x = torch.ones(g.volume_shape, dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    plan.mlem(p, x, plain_iters)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    r_plain, _ = plan.residual(p, x)
+    target = r_plain * (1.0 + tol)
+    # warm start
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x0, accepted, r_w, r_u = warm_start(plan, net, p)
+    n_w, r_end = iterations_to_residual(plan, p, x0, target, plain_iters)
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    reached = r_end is not None and r_end <= target
+    out = {"seed": seed, "plain_iters": plain_iters, "plain_s": t_plain, "plain_residual": r_plain,
+           "warm_accepted": accepted, "warm_start_residual": r_w, "uniform_start_residual": r_u,
+           "warm_iters": n_w, "warm_s": t_warm, "warm_residual": r_end, "reached": reached,
+           "speedup": t_plain / t_warm if reached else None}
+    plan.close()
+    return out
+
+
+def _cli():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("--out", default="warmstart_out")
+    ap.add_argument("--ckpt", default=None)
+    ap.add_argument("--triples", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--target-iters", type=int, default=100)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--crop", default="256,256,64")
+    ap.add_argument("--cases", type=int, default=50)
+    ap.add_argument("--case-size", default="1024,1024,128")
+    ap.add_argument("--seed", type=int, default=5000)
+    args = ap.parse_args()
+    import torch
+    os.makedirs(args.out, exist_ok=True)
+    ctx = engine.Context(0)
+    ctx.use_torch_stream()
+    net = engine.UNet(ctx, seed=args.seed)
+    report = {}
+    log = lambda s: print(s, flush=True)  # noqa: E731
+    if args.cmd == "train":
+        nx, ny, nz = (int(t) for t in args.crop.split(","))
+        g = crop_geometry(nx, ny, nz)
+        t0 = time.perf_counter()
+        triples = []
+        for i in range(args.triples):
+            s, x, _ = make_triple(ctx, g, ph.seed_for(5, i), target_iters=args.target_iters)
+            triples.append((s, x))
+        torch.cuda.synchronize()
+        t_gen = time.perf_counter() - t0
+        log(f"generated {len(triples)} triples in {t_gen:.1f} s")
+        t0 = time.perf_counter()
+        hist = train(net, triples, args.epochs, args.lr, log=log)
+        t_train = time.perf_counter() - t0
+        path = os.path.join(args.out, "unet.npz")
+        net.save(path)
+        report = {"triples": len(triples), "crop": [nx, ny, nz], "target_iters": args.target_iters,
+                  "epochs": args.epochs, "lr": args.lr, "generate_s": t_gen, "train_s": t_train,
+                  "loss_history": hist, "checkpoint": path}
+    else:
+        net.load(args.ckpt)
+        nx, ny, nz = (int(t) for t in args.case_size.split(","))
+        g = config_chest() if (nx, ny, nz) == (1024, 1024, 128) else \
+            linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, 60, 2 * nx, 2 * ny, 0.2, 0.2, 17.5)
+        cases = [evaluate_case(ctx, net, g, ph.seed_for(5, 100000 + i)) for i in range(args.cases)]
+        for c in cases:
+            log(json.dumps(c))
+        sp = [c["speedup"] for c in cases if c["speedup"]]
+        report = {"cases": cases, "case_size": [nx, ny, nz],
+                  "reached": sum(c["reached"] for c in cases), "accepted": sum(c["warm_accepted"] for c in cases),
+                  "median_speedup": float(np.median(sp)) if sp else None}
+    with open(os.path.join(args.out, f"{args.cmd}_report.json"), "w") as f:
+        json.dump(report, f, indent=1)
+    log(json.dumps({k: v for k, v in report.items() if k != "cases"}))
+
+
+if __name__ == "__main__":
+    _cli()
