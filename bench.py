@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-ttr", action="store_true",
+                    help="skip the learned-warm-start time-to-residual comparison")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip timing the reference's own CUDA kernels on a sample")
     ap.add_argument("--views", type=int, default=0,
                     help="keep only the first N views (smaller case for profiling captures)")
     return ap.parse_args()
@@ -230,6 +234,79 @@ def reference_arm(args, g, desc):
     print(json.dumps(line), flush=True)
 
 
+def reference_gpu(g, truth):
+    """The reference's own CUDA kernels (Projector.cu:227-785, compiled from
+    source by oracle/build_ref.sh) timed on this GPU on a sample of the
+    workload: the same volume and views 0, 1/3, 2/3 and last.  The forward
+    kernel runs on a central 256 x 256 detector ROI (it has no defined
+    result for rays that miss the volume, so the sample keeps every ray
+    inside it) and is extrapolated by rays; the backprojector runs on the
+    full detector and is extrapolated by views.  Kernel time only -- the
+    reference's per-call allocations, copies and host ratio/update loops are
+    not included."""
+    import dataclasses
+
+    import torch
+
+    from oracle import ref_gpu
+    if not ref_gpu.available("fma"):
+        return {"unavailable": "reference kernels not compiled (oracle/build_ref.sh needs the reference sources)"}
+    roi = 256
+    views = sorted({0, g.n_views // 3, (2 * g.n_views) // 3, g.n_views - 1})
+    det = g.det_origin.copy()
+    det[:, 0] += 0.5 * (g.nu - roi) * g.du
+    det[:, 1] += 0.5 * (g.nv - roi) * g.dv
+    gs = dataclasses.replace(g, nu=roi, nv=roi, det_origin=det).subset_views(views)
+    if not ref_gpu.all_rays_cross_volume(gs):
+        return {"unavailable": "sample geometry has rays that miss the volume"}
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    gb = g.subset_views(views)
+    ref_gpu.forward(gs, truth)                       # module load and warm-up
+    f_ms, _ = timed(lambda: ref_gpu.forward(gs, truth))
+    proj = torch.ones(gb.proj_shape, dtype=torch.float32, device=truth.device)
+    b_ms, _ = timed(lambda: ref_gpu.back(gb, proj))
+    fwd = f_ms * g.n_rays / gs.n_rays
+    back = b_ms * g.n_views / gb.n_views
+    return {"kind": "reference kernels compiled from source for sm_103a (nvcc defaults), run on this GPU",
+            "sample": f"views {views}: forward on a central {roi}x{roi} detector ROI {f_ms:.1f} ms, "
+                      f"backprojection (full detector) {b_ms:.1f} ms; extrapolated by rays / views",
+            "forward_ms": fwd, "back_ms": back, "iteration_ms": fwd + back,
+            "value": 2 * g.n_rays / ((fwd + back) * 1e-3), "unit": UNIT}
+
+
+WEIGHTS = os.path.join(ROOT, "kevernals_gb300", "weights", "unet_chest_dt.npz")
+
+
+def time_to_residual(ctx, g, cfg, rank, plain_iters=50):
+    """The headline comparison on the bench's own case (same seeded phantom
+    and Poisson data): plain GPU MLEM from the uniform start for
+    `plain_iters` iterations, against the learned warm start (shift-and-add
+    volume through the trained U-Net, kept only if its data residual is no
+    worse than the uniform start's) followed by MLEM until the plain
+    residual is reached within 1 %.  Wall time of each, sensitivity image
+    precomputed for both."""
+    from kevernals_gb300 import engine, phantom as ph, warmstart as ws
+    if not os.path.exists(WEIGHTS):
+        return {"unavailable": "no trained U-Net checkpoint in kevernals_gb300/weights/"}
+    net = engine.UNet(ctx, seed=0)
+    net.load(WEIGHTS)
+    r = ws.evaluate_case(ctx, net, g, ph.seed_for(cfg, rank), plain_iters=plain_iters)
+    net.close()
+    return {"plain_iters": plain_iters, "plain_s": r["plain_s"], "plain_residual": r["plain_residual"],
+            "warm_start_s": r["warm_start_s"], "warm_iters": r["warm_iters"], "warm_s": r["warm_s"],
+            "warm_residual": r["warm_residual"], "accepted": r["warm_accepted"], "reached": r["reached"],
+            "speedup": r["speedup"], "checkpoint": os.path.relpath(WEIGHTS, ROOT)}
+
+
 def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
     import torch
 
@@ -335,6 +412,13 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_exact(g, truth.cpu().numpy(), p.cpu().numpy(), args.cpu_seconds)
+    ref_gpu_line = reference_gpu(g, truth) if rank == 0 and not args.no_ref_gpu else None
+    ttr = None
+    if (not args.no_ttr and args.workload == "chest" and args.family == "exact"
+            and args.storage == "f32" and args.views == 0):
+        del x
+        plan.close()
+        ttr = time_to_residual(ctx, g, cfg, rank)
 
     if rank == 0:
         out = {
@@ -347,7 +431,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
                        "rays_per_step": rays_per_step, "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": gpu_launches, "roofline": roof,
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "reference_gpu": ref_gpu_line, "time_to_residual": ttr,
             "kernels": {k: {"launches": n, "avg_ms": t / n} for k, (n, t) in kernels.items()},
         }
         print(json.dumps(out), flush=True)

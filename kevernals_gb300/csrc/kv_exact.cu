@@ -120,56 +120,39 @@ __device__ __forceinline__ void fwd_tile(const ExGeom &G, const ExactTables &T, 
                 // Row segments of the (warp-uniform) y walk; inside each, the
                 // lane's x crossings.  Weights: same expressions as the
                 // backprojector's min(1, tx_hi, ty_hi) - max(0, tx_lo, ty_lo).
-                // Software-pipelined: the two voxels a row segment can touch
-                // (current column and the next one) are loaded one row ahead.
                 const VolT *ptr = slice + (size_t)(jb + j) * G.nx + (ib + i);
-                float cur0 = Store<VolT>::ld(ptr), cur1 = Store<VolT>::ld(ptr + mvx);
                 while (true) {
                     const float tb = fminf(ty, 1.0f);
                     const bool cross = tx < tb;
-                    const VolT *nptr = ptr + (cross ? mvx : 0) + step_y;   // first voxel of the next row
-                    float nxt0 = 0.f, nxt1 = 0.f;
-                    if (tb < 1.0f) {
-                        nxt0 = Store<VolT>::ld(nptr);
-                        nxt1 = Store<VolT>::ld(nptr + mvx);
-                    }
-                    // first piece of the row segment, in the current column
                     const float te = fminf(tx, tb);
                     const float w = __fsub_rn(te, t);
-                    acc = fmaf(w, cur0, acc);
+                    acc = fmaf(w, Store<VolT>::ld(ptr), acc);
                     if (MODE == FWD_SART) wsum += w;
-                    t = te;
-                    if (cross) {
-                        // the lane crosses a column inside this row segment
+                    // the common case -- at most one column crossing in the
+                    // row segment -- without a divergent branch
+                    float vc = cross ? Store<VolT>::ld(ptr + mvx) : 0.f;
+                    ptr += cross ? mvx : 0;
+                    fxp += cross ? fmvx : 0.f;
+                    tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
+                    float tc = te;
+                    while (tx < tb) {   // rarely: a second crossing in the same row
+                        const float w2 = __fsub_rn(tx, tc);
+                        acc = fmaf(w2, vc, acc);
+                        if (MODE == FWD_SART) wsum += w2;
+                        tc = tx;
                         ptr += mvx;
                         fxp += fmvx;
                         tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
-                        float cv = cur1;
-                        while (tx < tb) {   // rarely: a second crossing in the same row
-                            const float w2 = __fsub_rn(tx, t);
-                            acc = fmaf(w2, cv, acc);
-                            if (MODE == FWD_SART) wsum += w2;
-                            t = tx;
-                            ptr += mvx;
-                            fxp += fmvx;
-                            tx = __fmul_rn(__fsub_rn(fxp, ftx), X.z);
-                            cv = Store<VolT>::ld(ptr);
-                        }
-                        const float w3 = __fsub_rn(tb, t);
-                        acc = fmaf(w3, cv, acc);
-                        if (MODE == FWD_SART) wsum += w3;
-                        t = tb;
-                        if (tb < 1.0f && ptr + step_y != nptr) {   // after a second crossing
-                            nxt0 = Store<VolT>::ld(ptr + step_y);
-                            nxt1 = Store<VolT>::ld(ptr + step_y + mvx);
-                        }
+                        vc = Store<VolT>::ld(ptr);
                     }
+                    const float w3 = __fsub_rn(tb, tc);
+                    acc = fmaf(w3, vc, acc);
+                    if (MODE == FWD_SART) wsum += w3;
+                    t = tb;
                     if (tb >= 1.0f) break;
                     ptr += step_y;
                     fyp += fmvy;
                     ty = __fmul_rn(__fsub_rn(fyp, fty), Y.z);
-                    cur0 = nxt0;
-                    cur1 = nxt1;
                 }
             } else {
                 int ai = ib + i, aj = jb + j;
@@ -303,7 +286,12 @@ __global__ void prescale_kernel(ExGeom G, ExactTables T, const float *y, ProjT *
 // Gather backprojector.  Block = 32 x BY voxels (i fastest) of one slice k;
 // warp w owns row j.  For every view, each warp computes the slice-local
 // y-intervals of its candidate detector rows once into shared memory; each
-// lane then loops over the candidate columns u of its voxel.
+// lane holds the x-intervals of its voxel's candidate detector columns in
+// registers (up to BACK_SLOTS at a time) and accumulates over (candidate row,
+// candidate column), in a row loop unrolled for the warp's slot count.
+// (Computing the x-intervals once per block in shared memory instead -- they
+// depend on the column, not the row -- measured slower: the two block
+// barriers per view cost more than the redundant interval arithmetic.)
 // Accumulators of the backprojector: plain FP32, Kahan-compensated FP32 (the
 // reduced-precision storage modes), and a double-float sum of exact products
 // (TwoProduct + TwoSum in FP32 arithmetic, ~1e-14 relative) for the FP64
@@ -313,6 +301,43 @@ enum { ACC_F32 = 0, ACC_KAHAN = 1, ACC_DF = 2 };
 // Candidate detector columns a lane holds in registers at once (a voxel at
 // the chest-DT geometry has 4-7).
 constexpr int BACK_SLOTS = 8;
+
+// One backprojection term w * y into the accumulator (acc, comp).
+template <int ACC>
+__device__ __forceinline__ void back_accumulate(float w, float yv, float &acc, float &comp) {
+    if (ACC == ACC_KAHAN) {         // compensated (Kahan) summation
+        const float y_ = __fsub_rn(__fmul_rn(w, yv), comp);
+        const float t_ = __fadd_rn(acc, y_);
+        comp = __fsub_rn(__fsub_rn(t_, acc), y_);
+        acc = t_;
+    } else if (ACC == ACC_DF) {     // exact product + TwoSum: a double-float sum
+        const float pr = __fmul_rn(w, yv);
+        const float pe = __fmaf_rn(w, yv, -pr);
+        const float s_ = __fadd_rn(acc, pr);
+        const float bp = __fsub_rn(s_, acc);
+        const float er = __fadd_rn(__fsub_rn(acc, __fsub_rn(s_, bp)), __fsub_rn(pr, bp));
+        acc = s_;
+        comp = __fadd_rn(comp, __fadd_rn(er, pe));
+    } else {
+        acc = fmaf(w, yv, acc);
+    }
+}
+
+// The (candidate row, candidate column) terms of one voxel: nvc rows of
+// y-intervals ys[] against NS column slots of x-intervals in registers.
+template <int NS, typename ProjT, int ACC>
+__device__ __forceinline__ void back_rows(const ProjT *row, int nu, int nvc, const float2 *ys,
+                                          const float (&lox)[BACK_SLOTS], const float (&hix)[BACK_SLOTS],
+                                          float &acc, float &comp) {
+    for (int c = 0; c < nvc; ++c, row += nu) {
+        const float2 yi = ys[c];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const float w = __fsub_rn(fminf(hix[s], yi.y), fmaxf(lox[s], yi.x));
+            if (w > 0.f) back_accumulate<ACC>(w, Store<ProjT>::ld(row + s), acc, comp);
+        }
+    }
+}
 
 template <typename VolT, typename ProjT, int ACC, int MODE>
 __device__ __forceinline__ void back_tile(const ExGeom &G, const ExactTables &T, const BackArgs &a,
@@ -379,32 +404,16 @@ __device__ __forceinline__ void back_tile(const ExGeom &G, const ExactTables &T,
                         }
                     }
                     const ProjT *row = yp + ((size_t)p * G.nv + vb) * G.nu + ub;
-                    for (int c = 0; c < nvc; ++c, row += G.nu) {
-                        const float2 yi = ysh[warp][c];
-#pragma unroll
-                        for (int s = 0; s < BACK_SLOTS; ++s) {
-                            if (s >= nslot) break;
-                            const float w = __fsub_rn(fminf(hix[s], yi.y), fmaxf(lox[s], yi.x));
-                            if (w > 0.f) {
-                                const float yv = Store<ProjT>::ld(row + s);
-                                if (ACC == ACC_KAHAN) {         // compensated (Kahan) summation
-                                    const float y_ = __fsub_rn(__fmul_rn(w, yv), comp);
-                                    const float t_ = __fadd_rn(acc, y_);
-                                    comp = __fsub_rn(__fsub_rn(t_, acc), y_);
-                                    acc = t_;
-                                } else if (ACC == ACC_DF) {     // exact product + TwoSum: a double-float sum
-                                    const float pr = __fmul_rn(w, yv);
-                                    const float pe = __fmaf_rn(w, yv, -pr);
-                                    const float s_ = __fadd_rn(acc, pr);
-                                    const float bp = __fsub_rn(s_, acc);
-                                    const float er = __fadd_rn(__fsub_rn(acc, __fsub_rn(s_, bp)), __fsub_rn(pr, bp));
-                                    acc = s_;
-                                    comp = __fadd_rn(comp, __fadd_rn(er, pe));
-                                } else {
-                                    acc = fmaf(w, yv, acc);
-                                }
-                            }
-                        }
+                    // nslot is warp-uniform: one unrolled row loop per slot count
+                    switch (nslot) {
+                    case 1: back_rows<1, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 2: back_rows<2, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 3: back_rows<3, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 4: back_rows<4, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 5: back_rows<5, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 6: back_rows<6, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    case 7: back_rows<7, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
+                    default: back_rows<8, ProjT, ACC>(row, G.nu, nvc, ysh[warp], lox, hix, acc, comp); break;
                     }
                 }
                 __syncwarp();

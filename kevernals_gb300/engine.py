@@ -423,9 +423,23 @@ class UNet:
         return self.get_state()[0][: self.num_params]
 
     def save(self, path):
+        """Full training state (parameters and Adam moments)."""
         st, step = self.get_state()
         np.savez(path, state=st, step=step)
 
+    def save_weights(self, path):
+        """Parameters only (for inference; training resumes with fresh moments)."""
+        st, step = self.get_state()
+        np.savez_compressed(path, params=st[: self.num_params], step=step)
+
     def load(self, path):
+        """Loads a file written by save() or save_weights()."""
         z = np.load(path)
-        self.set_state(z["state"], int(z["step"]))
+        if "state" in z.files:
+            self.set_state(z["state"], int(z["step"]))
+            return
+        n = self.num_params
+        params = np.asarray(z["params"], np.float32)
+        if params.size != n:
+            raise ValueError(f"checkpoint holds {params.size} parameters, the network has {n}")
+        self.set_state(np.concatenate([params, np.zeros(2 * n, np.float32)]), int(z["step"]))

@@ -37,6 +37,47 @@ def crop_geometry(nx=256, ny=256, nz=64, n_views=60, half_angle=17.5) -> Geometr
     return linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, n_views, 1024, 1024, 0.2, 0.2, half_angle)
 
 
+def column_geometry(centre_mm, nx=128, ny=256, full: Geometry = None) -> Geometry:
+    """A full-thickness column of the chest-DT volume (nx x ny x 128 voxels,
+    the chest's voxel grid, centred laterally at `centre_mm` in the chest
+    frame, a multiple of the voxel pitch) seen by the chest's own sources and
+    detector pixels: per view, the detector ROI is the pixel box covering the
+    column's shadow (a common nu x nv for all views, per-view origins on the
+    chest's pixel grid).  The column problem's rays are chest rays; its
+    voxels are chest voxels."""
+    g = config_chest() if full is None else full
+    cx, cy = (round(float(c) / p) * p for c, p in zip(centre_mm, (g.dx, g.dy)))
+    hx, hy, hz = 0.5 * nx * g.dx, 0.5 * ny * g.dy, 0.5 * g.nz * g.dz
+    src = g.src.astype(np.float64)
+    det = g.det_origin.astype(np.float64)
+    zd = det[0, 2]
+    boxes = []
+    for p in range(g.n_views):
+        s = src[p]
+        pts = []
+        for x in (cx - hx, cx + hx):
+            for y in (cy - hy, cy + hy):
+                for z in (-hz, hz):
+                    a = (zd - s[2]) / (z - s[2])
+                    pts.append((s[0] + a * (x - s[0]), s[1] + a * (y - s[1])))
+        pts = np.asarray(pts)
+        u0 = int(np.floor((pts[:, 0].min() - det[p, 0]) / g.du)) - 1
+        u1 = int(np.ceil((pts[:, 0].max() - det[p, 0]) / g.du)) + 1
+        v0 = int(np.floor((pts[:, 1].min() - det[p, 1]) / g.dv)) - 1
+        v1 = int(np.ceil((pts[:, 1].max() - det[p, 1]) / g.dv)) + 1
+        boxes.append((u0, u1, v0, v1))
+    nu = max(b[1] - b[0] for b in boxes)
+    nv = max(b[3] - b[2] for b in boxes)
+    org = np.zeros((g.n_views, 3))
+    for p, (u0, u1, v0, v1) in enumerate(boxes):
+        ua = min(max(u0 - (nu - (u1 - u0)) // 2, 0), g.nu - nu)   # common size, inside the chest detector
+        va = min(max(v0 - (nv - (v1 - v0)) // 2, 0), g.nv - nv)
+        org[p] = (det[p, 0] + ua * g.du - cx, det[p, 1] + va * g.dv - cy, zd)
+    src_c = src - np.array([cx, cy, 0.0])
+    return Geometry(nx, ny, g.nz, g.dx, g.dy, g.dz, nu, nv, g.du, g.dv, src_c, org,
+                    fulcrum_z=g.fulcrum_z), (cx, cy)
+
+
 def noisy_data(ctx, plan, truth, i0, seed):
     import torch
     line = plan.forward(truth)
@@ -53,10 +94,40 @@ def shift_and_add_volume(plan, p):
     return x
 
 
-def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100):
-    """(shift-and-add, MLEM target, data) for one seeded phantom, on the GPU."""
+def window_params(seed, offset_mm, n_ellipsoids=400):
+    """Ellipsoids of a seeded chest-DT phantom (1024 x 1024 x 128 at
+    0.4 x 0.4 x 2.5 mm, `n_ellipsoids` plus the background) re-centred so
+    that a crop volume centred at the origin shows the window of that
+    phantom centred at `offset_mm` (chest frame): the training crops see
+    structures of the sizes the chest-DT volumes hold."""
+    params = ph.ellipsoid_params(1024, 1024, 128, 0.4, 0.4, 2.5, n_ellipsoids, seed).copy()
+    params[:, 0:3] -= np.asarray(offset_mm, np.float32)
+    return params
+
+
+def column_centre(seed, nx=128, ny=256):
+    """A seeded column centre (mm, chest frame) inside 0.8 x the room the
+    chest-DT volume leaves around an nx x ny column."""
+    rng = ph.SplitMix64(seed ^ 0x2545F4914F6CDD1D)
+    room = (0.5 * (1024 - nx) * 0.4, 0.5 * (1024 - ny) * 0.4)
+    return [rng.uniform(-0.8 * r, 0.8 * r) for r in room]
+
+
+def window_offset(seed, crop: Geometry):
+    """A seeded window centre inside 0.8 x the room the chest-DT volume
+    leaves around the crop."""
+    rng = ph.SplitMix64(seed ^ 0x5DEECE66D)
+    room = [0.5 * (1024 * 0.4 - crop.nx * crop.dx), 0.5 * (1024 * 0.4 - crop.ny * crop.dy),
+            0.5 * (128 * 2.5 - crop.nz * crop.dz)]
+    return [rng.uniform(-0.8 * r, 0.8 * r) if r > 0 else 0.0 for r in room]
+
+
+def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100, params=None):
+    """(shift-and-add, MLEM target, data) for one seeded phantom, on the GPU;
+    `params` (ellipsoid rows) overrides the phantom drawn for g."""
     import torch
-    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
+    if params is None:
+        params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
     truth = engine.phantom(ctx, g, params, device=True)
     plan = engine.Plan(ctx, g, "exact")
     p = noisy_data(ctx, plan, truth, i0, seed)
@@ -68,7 +139,7 @@ def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100):
     return s, x, p
 
 
-def train(net, triples, epochs, lr=1e-3, seed=0, log=None):
+def train(net, triples, epochs, lr=1e-3, seed=0, log=None, on_epoch=None):
     rng = np.random.default_rng(seed)
     history = []
     for ep in range(epochs):
@@ -77,6 +148,8 @@ def train(net, triples, epochs, lr=1e-3, seed=0, log=None):
         history.append(float(np.mean(losses)))
         if log:
             log(f"epoch {ep + 1}/{epochs}: mean loss {history[-1]:.4e}")
+        if on_epoch:
+            on_epoch(ep, history)
     return history
 
 
@@ -130,13 +203,16 @@ def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipso
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     x0, accepted, r_w, r_u = warm_start(plan, net, p)
+    torch.cuda.synchronize()
+    t_start = time.perf_counter() - t0
     n_w, r_end = iterations_to_residual(plan, p, x0, target, plain_iters)
     torch.cuda.synchronize()
     t_warm = time.perf_counter() - t0
     reached = r_end is not None and r_end <= target
     out = {"seed": seed, "plain_iters": plain_iters, "plain_s": t_plain, "plain_residual": r_plain,
            "warm_accepted": accepted, "warm_start_residual": r_w, "uniform_start_residual": r_u,
-           "warm_iters": n_w, "warm_s": t_warm, "warm_residual": r_end, "reached": reached,
+           "warm_start_s": t_start, "warm_iters": n_w, "warm_s": t_warm, "warm_residual": r_end,
+           "reached": reached,
            "speedup": t_plain / t_warm if reached else None}
     plan.close()
     return out
@@ -151,10 +227,15 @@ def _cli():
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--target-iters", type=int, default=100)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--crop", default="256,256,64")
+    ap.add_argument("--crop", default="128,256",
+                    help="training volume nx,ny[,nz] (nz only for the centred crop geometries)")
     ap.add_argument("--cases", type=int, default=50)
     ap.add_argument("--case-size", default="1024,1024,128")
     ap.add_argument("--seed", type=int, default=5000)
+    ap.add_argument("--phantom", choices=["column", "window", "crop"], default="column",
+                    help="training cases: full-thickness columns of chest-DT phantoms seen by the chest "
+                         "geometry's own rays (--crop gives nx,ny), windows of chest-DT phantoms in the "
+                         "centred crop geometry, or phantoms drawn for the crop")
     args = ap.parse_args()
     import torch
     os.makedirs(args.out, exist_ok=True)
@@ -164,24 +245,50 @@ def _cli():
     report = {}
     log = lambda s: print(s, flush=True)  # noqa: E731
     if args.cmd == "train":
-        nx, ny, nz = (int(t) for t in args.crop.split(","))
+        dims = [int(t) for t in args.crop.split(",")]
+        nx, ny = dims[0], dims[1]
+        nz = dims[2] if len(dims) > 2 else 128
         g = crop_geometry(nx, ny, nz)
         t0 = time.perf_counter()
         triples = []
         for i in range(args.triples):
-            s, x, _ = make_triple(ctx, g, ph.seed_for(5, i), target_iters=args.target_iters)
+            seed = ph.seed_for(5, i)
+            params = None
+            if args.phantom == "column":
+                g, centre = column_geometry(column_centre(seed, nx, ny), nx, ny)
+                nz = g.nz
+                params = window_params(seed, (centre[0], centre[1], 0.0))
+            elif args.phantom == "window":
+                params = window_params(seed, window_offset(seed, g))
+            s, x, _ = make_triple(ctx, g, seed, target_iters=args.target_iters, params=params)
             triples.append((s, x))
+            if (i + 1) % 50 == 0:
+                log(f"{i + 1} triples, {time.perf_counter() - t0:.1f} s")
         torch.cuda.synchronize()
         t_gen = time.perf_counter() - t0
         log(f"generated {len(triples)} triples in {t_gen:.1f} s")
         t0 = time.perf_counter()
-        hist = train(net, triples, args.epochs, args.lr, log=log)
-        t_train = time.perf_counter() - t0
         path = os.path.join(args.out, "unet.npz")
-        net.save(path)
+        n_val = max(1, len(triples) // 16)
+        val, triples = triples[-n_val:], triples[:-n_val]
+
+        def validate():
+            mse_net = np.mean([float(((net.forward(a) - b) ** 2).mean()) for a, b in val])
+            mse_id = np.mean([float(((a - b) ** 2).mean()) for a, b in val])
+            return float(mse_net), float(mse_id)
+
+        val_hist = []
+
+        def on_epoch(ep, h):
+            net.save(path)
+            val_hist.append(validate())
+            log(f"  held-out MSE: network {val_hist[-1][0]:.4e}, shift-and-add itself {val_hist[-1][1]:.4e}")
+        hist = train(net, triples, args.epochs, args.lr, log=log, on_epoch=on_epoch)
+        t_train = time.perf_counter() - t0
         report = {"triples": len(triples), "crop": [nx, ny, nz], "target_iters": args.target_iters,
+                  "phantom": args.phantom,
                   "epochs": args.epochs, "lr": args.lr, "generate_s": t_gen, "train_s": t_train,
-                  "loss_history": hist, "checkpoint": path}
+                  "loss_history": hist, "held_out_mse": val_hist, "checkpoint": path}
     else:
         net.load(args.ckpt)
         nx, ny, nz = (int(t) for t in args.case_size.split(","))

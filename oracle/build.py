@@ -4,7 +4,8 @@ liboracle.so   kvtomo_oracle.c, gcc -O2 -fopenmp -ffp-contract=off (no fused
                multiply-add, so the RC restatement is bit-identical to the
                reference kernels compiled for the host).
 _ref/libkvref.so  the reference's own kernels, compiled from the reference
-               tree by build_ref.sh when that tree is present.
+               tree by build_ref.sh when that tree is present (with the
+               GPU cubins _ref/ref_kernels*.cubin, see ref_gpu.py).
 """
 import os
 import subprocess
@@ -30,7 +31,8 @@ def build_ref(force=False):
     """Compiles the reference kernels when the reference tree is present."""
     if not os.path.isdir(REFERENCE_ROOT):
         return None
-    if not force and os.path.exists(REF_SO):
+    cubins = [os.path.join(HERE, "_ref", f) for f in ("ref_kernels.cubin", "ref_kernels_nofma.cubin")]
+    if not force and os.path.exists(REF_SO) and all(os.path.exists(c) for c in cubins):
         return REF_SO
     subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
     return REF_SO if os.path.exists(REF_SO) else None

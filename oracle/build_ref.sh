@@ -1,8 +1,14 @@
 #!/usr/bin/env bash
-# Builds oracle/_ref/libkvref.so: the reference's own projector kernels
+# Builds, from the reference's own projector kernels
 # (source/modules/reconstruction/Projector.cu, lines 22-785: the device and
-# global functions, no host code) compiled for the CPU through ref_shim.h.
-# TEST INFRASTRUCTURE: a checker for the RC restatement in kvtomo_oracle.c.
+# global functions, no host code):
+#   oracle/_ref/libkvref.so          compiled for the CPU through ref_shim.h
+#   oracle/_ref/ref_kernels.cubin    compiled for sm_103a as the reference
+#                                    ships them (nvcc defaults, FMA contraction on)
+#   oracle/_ref/ref_kernels_nofma.cubin  the same with -fmad=false
+# (the cubins only when nvcc is on PATH).
+# TEST INFRASTRUCTURE: checkers for the RC restatement in kvtomo_oracle.c and
+# for the engine's RC kernels, and the "reference GPU" timing line.
 #
 # Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
 # The kernel lines are extracted into oracle/_ref/ only for the compile and
@@ -23,3 +29,13 @@ g++ -std=c++17 -O2 -fPIC -shared -fopenmp -fpermissive -ffp-contract=off -w \
     -I "$here" -I "$out" "$here/ref_driver.cpp" -o "$out/libkvref.so"
 rm -f "$out/ref_kernels_cpu.inc"
 echo "build_ref: built $out/libkvref.so"
+if command -v nvcc > /dev/null; then
+    sed -n '22,785p' "$src" > "$out/ref_kernels_gpu.inc"
+    nvcc -std=c++17 -O3 -cubin -gencode arch=compute_103a,code=sm_103a -w \
+        -I "$out" "$here/ref_gpu_wrap.cu" -o "$out/ref_kernels.cubin" &
+    nvcc -std=c++17 -O3 -cubin -gencode arch=compute_103a,code=sm_103a -w -fmad=false \
+        -I "$out" "$here/ref_gpu_wrap.cu" -o "$out/ref_kernels_nofma.cubin" &
+    wait
+    rm -f "$out/ref_kernels_gpu.inc"
+    echo "build_ref: built $out/ref_kernels.cubin, $out/ref_kernels_nofma.cubin"
+fi

@@ -166,3 +166,26 @@ def test_config1_digests_from_reference():
     d = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
     assert d(vol) == info["phantom_sha256"]
     assert d(O.rc_forward(g, vol)) == info["ref_forward_sha256"]
+
+
+def test_reference_gpu_guard_agrees_with_reference_hit_test():
+    """oracle/ref_gpu.py launches the reference forward kernel only on
+    geometries where every ray crosses the volume (the kernel has no defined
+    result for a missed ray, Projector.cu:79-85).  Its host guard must never
+    accept a geometry in which the reference's own hit test
+    (FindProjectionAlphas_d's box clip, restated as kvo_rc_ray_hits) misses a
+    ray, and it must refuse the config-1 geometry, whose detector extends
+    past the volume's shadow."""
+    from oracle import ref_gpu
+    lib = O.lib()
+    accepted = [linear_sweep(256, 256, 64, 0.5, 0.5, 1.0, 15, 224, 224, 0.4, 0.4, 15.0),
+                linear_sweep(64, 48, 16, 0.5, 0.5, 1.0, 5, 40, 30, 0.4, 0.4, 10.0)]
+    for g in accepted:
+        assert ref_gpu.all_rays_cross_volume(g)
+        cg = O.cgeom(g)
+        for p in range(g.n_views):
+            for v in range(0, g.nv, 3):
+                for u in range(0, g.nu, 3):
+                    assert lib.kvo_rc_ray_hits(cg, p, u, v)
+    assert not ref_gpu.all_rays_cross_volume(config_small())
+    assert not ref_gpu.all_rays_cross_volume(linear_sweep(64, 48, 16, 0.5, 0.5, 1.0, 5, 80, 60, 0.4, 0.4, 20.0))
