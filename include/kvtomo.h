@@ -202,7 +202,9 @@ size_t kv_unet_num_params(const kv_unet *net);
 kv_status kv_unet_forward(kv_unet *net, const float *in, float *out, int32_t D, int32_t H, int32_t W,
                           kv_mem mem);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the mean squared error
- * between net(in) and target; *loss is the loss before the step. */
+ * between net(in) and target; *loss is the loss before the step.  Target
+ * voxels that are NaN carry no target: they add nothing to the loss (which
+ * stays a sum over the other voxels divided by D*H*W). */
 kv_status kv_unet_train_step(kv_unet *net, const float *in, const float *target, int32_t D, int32_t H,
                              int32_t W, float lr, float *loss, kv_mem mem);
 /* Loss and FP32 parameter gradients (host buffer of kv_unet_num_params). */

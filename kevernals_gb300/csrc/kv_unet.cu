@@ -16,6 +16,7 @@
 //   y = x + conv1x1(d1: 16 -> 1)     (FP32 output)
 // pool = 2x2x2 average, up = nearest x2, ++ = channel concatenation (read in
 // place by the convolution, never copied).
+#include "kv_conv_tc.cuh"
 #include "kv_internal.h"
 #include "kv_unet_kernels.cuh"
 
@@ -110,13 +111,19 @@ __global__ void conv_out_fwd(const bf16 *__restrict__ h, const float *__restrict
     }
 }
 
-// loss partials: sum (y - t)^2 per block; dy = 2 (y - t) / n
+// loss partials: sum (y - t)^2 per block; dy = 2 (y - t) / n.  A NaN target
+// marks a voxel without a target: it adds nothing to the loss or gradient.
 __global__ void mse_loss(const float *__restrict__ y, const float *__restrict__ t, float *__restrict__ dy, long long n,
                          double *__restrict__ partials) {
     double s = 0.0;
     const float scale = 2.f / (float)n;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        const float d = y[v] - t[v];
+        const float tv = t[v];
+        if (tv != tv) {
+            dy[v] = 0.f;
+            continue;
+        }
+        const float d = y[v] - tv;
         s += (double)d * (double)d;
         dy[v] = scale * d;
     }
@@ -318,6 +325,7 @@ struct kv_unet {
     float *x = nullptr, *t = nullptr, *y = nullptr, *dy = nullptr, *loss = nullptr;
     double *partials = nullptr;
     float *corr = nullptr;                                          // Adam bias corrections (device)
+    int *tc_status = nullptr;                                       // tensor-core convolution wait status
     cudaGraphExec_t train_graph = nullptr;
     float graph_lr = 0.f;
 };
@@ -405,6 +413,18 @@ kv_status conv3(kv_unet *u, int layer, const bf16 *in1, const bf16 *in2, bf16 *o
     const float *bias = weights_t ? nullptr : u->p + L.b;
     const int blocks = (int)((nvox / 16 + 3) / 4);
     LaunchTimer lt(ctx, weights_t ? "unet_conv_dgrad" : "unet_conv_fwd");
+    int bw, bh, bd;
+    if (c1 + c2 >= 32 && cout >= 32 && convtc::tile_shape(D, H, W, bw, bh, bd)) {
+        // tcgen05 / TMA implicit GEMM (kv_conv_tc.cuh)
+        const char *why = convtc::launch(in1, c1, in2, c2, w, bias, !weights_t, out, cout, D, H, W, u->tc_status,
+                                         ctx->sm_count, ctx->stream);
+        if (why != nullptr) return kv_fail(ctx, KV_ERR_UNSUPPORTED, "tensor-core convolution: %s", why);
+        KV_CHECK_LAUNCH(ctx, "unet conv3 (tcgen05)");
+        return KV_OK;
+    }
+    // 16-channel convolutions, and volumes smaller than one 128-voxel tile:
+    // warp-level mma.sync (a 128 x 16 x 16 tcgen05 MMA per tap is too little
+    // work per TMA load to pay)
     for (int n0 = 0; n0 < cout; n0 += 64) {
         const int nc = cout - n0 < 64 ? cout - n0 : 64;
         const bool relu = !weights_t;
@@ -639,12 +659,14 @@ extern "C" kv_status kv_unet_create(kv_ctx *ctx, uint64_t seed, kv_unet **out) {
         cudaMalloc((void **)&u->v, off * sizeof(float)) != cudaSuccess ||
         cudaMalloc((void **)&u->pb, off * sizeof(bf16)) != cudaSuccess ||
         cudaMalloc((void **)&u->wt, off * sizeof(bf16)) != cudaSuccess ||
-        cudaMalloc((void **)&u->corr, 4 * sizeof(float)) != cudaSuccess) {
+        cudaMalloc((void **)&u->corr, 4 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void **)&u->tc_status, sizeof(int)) != cudaSuccess) {
         s = kv_fail(ctx, KV_ERR_OOM, "U-Net parameters");
     } else {
         cudaMemcpy(u->p, h.data(), off * sizeof(float), cudaMemcpyHostToDevice);
         cudaMemset(u->m, 0, off * sizeof(float));
         cudaMemset(u->v, 0, off * sizeof(float));
+        cudaMemset(u->tc_status, 0, sizeof(int));
         to_bf16<<<grid_n(ctx, (long long)off), 256, 0, ctx->stream>>>(u->p, u->pb, off);
         if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) s = kv_fail(ctx, KV_ERR_CUDA, "U-Net init");
     }
@@ -669,12 +691,29 @@ extern "C" kv_status kv_unet_destroy(kv_unet *u) {
     cudaFree(u->pb);
     cudaFree(u->wt);
     cudaFree(u->corr);
+    cudaFree(u->tc_status);
     delete u;
     kv_ctx_release_ref(ctx);
     return KV_OK;
 }
 
 extern "C" size_t kv_unet_num_params(const kv_unet *u) { return u ? u->nparams : 0; }
+
+namespace {
+// Reads (and clears) the tensor-core convolution's wait status: non-zero when
+// one of its bounded pipeline waits gave up.  Synchronises the stream.
+kv_status tc_check(kv_unet *u) {
+    kv_ctx *ctx = u->ctx;
+    int h = 0;
+    KV_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, u->tc_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h != 0) {
+        cudaMemset(u->tc_status, 0, sizeof(int));
+        return kv_fail(ctx, KV_ERR_TIMEOUT, "tensor-core convolution: pipeline wait %d timed out", h);
+    }
+    return KV_OK;
+}
+}  // namespace
 
 extern "C" kv_status kv_unet_forward(kv_unet *u, const float *in, float *out, int32_t D, int32_t H, int32_t W,
                                      kv_mem mem) {
@@ -687,8 +726,7 @@ extern "C" kv_status kv_unet_forward(kv_unet *u, const float *in, float *out, in
     KV_TRY(forward(u));
     KV_CHECK_CUDA(ctx, cudaMemcpyAsync(out, u->y, n * sizeof(float),
                                        mem == KV_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx->stream));
-    if (mem == KV_MEM_HOST) KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return KV_OK;
+    return tc_check(u);
 }
 
 // One Adam step on (input, target); loss = mean squared error before the step.
@@ -739,11 +777,8 @@ extern "C" kv_status kv_unet_train_step(kv_unet *u, const float *in, const float
         KV_CHECK_CUDA(ctx, cudaGraphLaunch(u->train_graph, ctx->stream));
     }
     u->step += 1;
-    if (loss) {
-        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(loss, u->loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-        KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    }
-    return KV_OK;
+    if (loss) KV_CHECK_CUDA(ctx, cudaMemcpyAsync(loss, u->loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    return tc_check(u);
 }
 
 // Loss and FP32 parameter gradients (no update), for gradient checks.
@@ -759,8 +794,7 @@ extern "C" kv_status kv_unet_gradients(kv_unet *u, const float *in, const float 
     KV_TRY(train_body(u, 0.f, false));
     KV_CHECK_CUDA(ctx, cudaMemcpyAsync(grads, u->g, u->nparams * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     if (loss) KV_CHECK_CUDA(ctx, cudaMemcpyAsync(loss, u->loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return KV_OK;
+    return tc_check(u);
 }
 
 // State = parameters, Adam first and second moments (3 * num_params floats)

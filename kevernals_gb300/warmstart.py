@@ -78,6 +78,19 @@ def column_geometry(centre_mm, nx=128, ny=256, full: Geometry = None) -> Geometr
                     fulcrum_z=g.fulcrum_z), (cx, cy)
 
 
+def chest_crops(s, x, nx, ny, n, seed):
+    """n seeded full-thickness nx x ny crops (input, target) of a whole-volume
+    triple; crop corners anywhere in the volume (edges included)."""
+    rng = ph.SplitMix64(seed ^ 0x9E3779B97F4A7C15)
+    D, H, W = s.shape
+    out = []
+    for _ in range(n):
+        x0 = min(int(rng.uniform(0, W - nx + 1)), W - nx)
+        y0 = min(int(rng.uniform(0, H - ny + 1)), H - ny)
+        out.append((s[:, y0:y0 + ny, x0:x0 + nx].contiguous(), x[:, y0:y0 + ny, x0:x0 + nx].contiguous()))
+    return out
+
+
 def noisy_data(ctx, plan, truth, i0, seed):
     import torch
     line = plan.forward(truth)
@@ -106,11 +119,28 @@ def window_params(seed, offset_mm, n_ellipsoids=400):
 
 
 def column_centre(seed, nx=128, ny=256):
-    """A seeded column centre (mm, chest frame) inside 0.8 x the room the
-    chest-DT volume leaves around an nx x ny column."""
+    """A seeded column centre (mm, chest frame) anywhere in the room the
+    chest-DT volume leaves around an nx x ny column (so columns also cover
+    the phantom's outer boundary and the empty corners)."""
     rng = ph.SplitMix64(seed ^ 0x2545F4914F6CDD1D)
     room = (0.5 * (1024 - nx) * 0.4, 0.5 * (1024 - ny) * 0.4)
-    return [rng.uniform(-0.8 * r, 0.8 * r) for r in room]
+    return [rng.uniform(-r, r) for r in room]
+
+
+# Lateral margin (voxels) of a column whose MLEM target is not used for
+# training: the column's side faces cut through tissue, and MLEM piles up
+# values there that the full volume does not have.
+COLUMN_MARGIN = 8
+
+
+def mask_margin(x, margin=COLUMN_MARGIN):
+    """The target with its lateral margin set to NaN (no target there)."""
+    t = x.clone()
+    t[:, :, :margin] = float("nan")
+    t[:, :, -margin:] = float("nan")
+    t[:, :margin, :] = float("nan")
+    t[:, -margin:, :] = float("nan")
+    return t
 
 
 def window_offset(seed, crop: Geometry):
@@ -181,11 +211,14 @@ def iterations_to_residual(plan, p, x, target, max_iters):
     return state["n"], state["r"]
 
 
-def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipsoids=400):
+def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipsoids=400, params=None,
+                  max_iters=None):
     """Plain MLEM (uniform start, plain_iters iterations) vs the warm start
-    reaching the same data residual within `tol`: iterations and wall time."""
+    reaching the same data residual within `tol` (at most `max_iters`
+    iterations, default plain_iters): iterations and wall time."""
     import torch
-    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
+    if params is None:
+        params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
     truth = engine.phantom(ctx, g, params, device=True)
     plan = engine.Plan(ctx, g, "exact")
     p = noisy_data(ctx, plan, truth, i0, seed)
@@ -205,7 +238,7 @@ def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipso
     x0, accepted, r_w, r_u = warm_start(plan, net, p)
     torch.cuda.synchronize()
     t_start = time.perf_counter() - t0
-    n_w, r_end = iterations_to_residual(plan, p, x0, target, plain_iters)
+    n_w, r_end = iterations_to_residual(plan, p, x0, target, max_iters or plain_iters)
     torch.cuda.synchronize()
     t_warm = time.perf_counter() - t0
     reached = r_end is not None and r_end <= target
@@ -226,16 +259,23 @@ def _cli():
     ap.add_argument("--triples", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--target-iters", type=int, default=100)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--crop", default="128,256",
                     help="training volume nx,ny[,nz] (nz only for the centred crop geometries)")
     ap.add_argument("--cases", type=int, default=50)
     ap.add_argument("--case-size", default="1024,1024,128")
+    ap.add_argument("--case-kind", choices=["volume", "column"], default="volume",
+                    help="evaluation cases: whole volumes of --case-size, or held-out chest-DT columns "
+                         "(--case-size gives nx,ny)")
+    ap.add_argument("--max-iters", type=int, default=None,
+                    help="most MLEM iterations the warm start may take (default: the plain count)")
     ap.add_argument("--seed", type=int, default=5000)
-    ap.add_argument("--phantom", choices=["column", "window", "crop"], default="column",
-                    help="training cases: full-thickness columns of chest-DT phantoms seen by the chest "
-                         "geometry's own rays (--crop gives nx,ny), windows of chest-DT phantoms in the "
-                         "centred crop geometry, or phantoms drawn for the crop")
+    ap.add_argument("--phantom", choices=["chest", "column", "window", "crop"], default="chest",
+                    help="training cases: crops (--crop gives nx,ny; full thickness) of whole chest-DT "
+                         "triples (--triples of them, --crops-per-volume crops each), full-thickness "
+                         "columns of chest-DT phantoms seen by the chest geometry's own rays, windows of "
+                         "chest-DT phantoms in the centred crop geometry, or phantoms drawn for the crop")
+    ap.add_argument("--crops-per-volume", type=int, default=16)
     args = ap.parse_args()
     import torch
     os.makedirs(args.out, exist_ok=True)
@@ -254,6 +294,14 @@ def _cli():
         for i in range(args.triples):
             seed = ph.seed_for(5, i)
             params = None
+            if args.phantom == "chest":
+                gc = config_chest()
+                s, x, _ = make_triple(ctx, gc, seed, n_ellipsoids=400, target_iters=args.target_iters)
+                triples.extend(chest_crops(s, x, nx, ny, args.crops_per_volume, seed))
+                del s, x
+                if (i + 1) % 4 == 0:
+                    log(f"{i + 1} chest triples, {time.perf_counter() - t0:.1f} s")
+                continue
             if args.phantom == "column":
                 g, centre = column_geometry(column_centre(seed, nx, ny), nx, ny)
                 nz = g.nz
@@ -261,7 +309,7 @@ def _cli():
             elif args.phantom == "window":
                 params = window_params(seed, window_offset(seed, g))
             s, x, _ = make_triple(ctx, g, seed, target_iters=args.target_iters, params=params)
-            triples.append((s, x))
+            triples.append((s, mask_margin(x) if args.phantom == "column" else x))
             if (i + 1) % 50 == 0:
                 log(f"{i + 1} triples, {time.perf_counter() - t0:.1f} s")
         torch.cuda.synchronize()
@@ -273,8 +321,11 @@ def _cli():
         val, triples = triples[-n_val:], triples[:-n_val]
 
         def validate():
-            mse_net = np.mean([float(((net.forward(a) - b) ** 2).mean()) for a, b in val])
-            mse_id = np.mean([float(((a - b) ** 2).mean()) for a, b in val])
+            def mse(a, b):
+                d = (a - b) ** 2
+                return float(d[~torch.isnan(d)].mean())
+            mse_net = np.mean([mse(net.forward(a), b) for a, b in val])
+            mse_id = np.mean([mse(a, b) for a, b in val])
             return float(mse_net), float(mse_id)
 
         val_hist = []
@@ -286,15 +337,23 @@ def _cli():
         hist = train(net, triples, args.epochs, args.lr, log=log, on_epoch=on_epoch)
         t_train = time.perf_counter() - t0
         report = {"triples": len(triples), "crop": [nx, ny, nz], "target_iters": args.target_iters,
-                  "phantom": args.phantom,
+                  "phantom": args.phantom, "volumes": args.triples,
                   "epochs": args.epochs, "lr": args.lr, "generate_s": t_gen, "train_s": t_train,
                   "loss_history": hist, "held_out_mse": val_hist, "checkpoint": path}
     else:
         net.load(args.ckpt)
         nx, ny, nz = (int(t) for t in args.case_size.split(","))
-        g = config_chest() if (nx, ny, nz) == (1024, 1024, 128) else \
-            linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, 60, 2 * nx, 2 * ny, 0.2, 0.2, 17.5)
-        cases = [evaluate_case(ctx, net, g, ph.seed_for(5, 100000 + i)) for i in range(args.cases)]
+        cases = []
+        for i in range(args.cases):
+            seed = ph.seed_for(5, 100000 + i)
+            if args.case_kind == "column":
+                g, centre = column_geometry(column_centre(seed, nx, ny), nx, ny)
+                params = window_params(seed, (centre[0], centre[1], 0.0))
+                cases.append(evaluate_case(ctx, net, g, seed, params=params, max_iters=args.max_iters))
+            else:
+                g = config_chest() if (nx, ny, nz) == (1024, 1024, 128) else \
+                    linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, 60, 2 * nx, 2 * ny, 0.2, 0.2, 17.5)
+                cases.append(evaluate_case(ctx, net, g, seed, max_iters=args.max_iters))
         for c in cases:
             log(json.dumps(c))
         sp = [c["speedup"] for c in cases if c["speedup"]]
