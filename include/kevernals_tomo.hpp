@@ -11,9 +11,13 @@
 // Differences, by design:
 //   * ImageDataPtr is a small reference-counted headless image (dimensions,
 //     spacing, origin, float32 buffer) instead of vtkSmartPointer<vtkImageData>.
-//   * TomoGeometry is built from values (the XML reader is not part of this
-//     layer); it keeps the reference's conventions: volume-centred frame,
-//     common source x/z and detector z, one ROI size and pixel spacing.
+//   * TomoGeometry is built from values, or read from the reference's XML
+//     geometry files (TomoGeometry(path), source/modules/geometry/
+//     TomoGeometry.cpp:13-434) by a small XML reader of this header; it keeps
+//     the reference's conventions: volume-centred frame, common source x/z
+//     and detector z, one ROI size and pixel spacing.  An unreadable file
+//     gives an invalid geometry (IsValid() false, ErrorMessage() says why)
+//     instead of the reference's console message.
 //   * Projector takes an operator family: KV_FAMILY_RC (default) reproduces
 //     the reference kernels; KV_FAMILY_EXACT is the Siddon line integral and
 //     its exact transpose.
@@ -22,9 +26,11 @@
 //     without `inline`).
 #pragma once
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <sstream>
 #include <memory>
 #include <optional>
 #include <stdexcept>
@@ -158,8 +164,260 @@ using ImageDataPtr = std::shared_ptr<ImageData>;
 
 // ---------------------------------------------------------------- geometry
 
+// ---------------------------------------------------------------- XML
+
+namespace kvxml {
+
+// A minimal XML element tree: element names, concatenated character data,
+// child elements.  Enough for the geometry files (no namespaces, DTDs or
+// processing of attributes, which those files do not use).
+struct Node {
+    std::string name, text;
+    std::vector<Node> children;
+    const Node *child(const std::string &n) const {
+        for (const auto &c : children)
+            if (c.name == n) return &c;
+        return nullptr;
+    }
+};
+
+class Parser {
+public:
+    explicit Parser(const std::string &src) : s_(src) {}
+    bool parse(Node &root, std::string &err) {
+        skip_misc();
+        return element(root, err);
+    }
+
+private:
+    const std::string &s_;
+    size_t i_ = 0;
+    bool starts(const char *t) const { return s_.compare(i_, std::char_traits<char>::length(t), t) == 0; }
+    void skip_ws() {
+        while (i_ < s_.size() && std::isspace(static_cast<unsigned char>(s_[i_]))) ++i_;
+    }
+    bool skip_past(const char *t) {
+        const size_t k = s_.find(t, i_);
+        if (k == std::string::npos) return false;
+        i_ = k + std::char_traits<char>::length(t);
+        return true;
+    }
+    // declarations, comments, doctype before the root element
+    void skip_misc() {
+        for (;;) {
+            skip_ws();
+            if (starts("<?")) { if (!skip_past("?>")) return; }
+            else if (starts("<!--")) { if (!skip_past("-->")) return; }
+            else if (starts("<!")) { if (!skip_past(">")) return; }
+            else return;
+        }
+    }
+    static void decode(std::string &t) {
+        static const std::pair<const char *, char> ents[] = {
+            {"&lt;", '<'}, {"&gt;", '>'}, {"&quot;", '"'}, {"&apos;", '\''}, {"&amp;", '&'}};
+        for (const auto &e : ents) {
+            size_t k;
+            const size_t n = std::char_traits<char>::length(e.first);
+            while ((k = t.find(e.first)) != std::string::npos) t.replace(k, n, 1, e.second);
+        }
+    }
+    bool element(Node &n, std::string &err) {
+        if (!starts("<")) { err = "expected an element"; return false; }
+        ++i_;
+        const size_t b = i_;
+        while (i_ < s_.size() && !std::isspace(static_cast<unsigned char>(s_[i_])) && s_[i_] != '>' && s_[i_] != '/')
+            ++i_;
+        n.name = s_.substr(b, i_ - b);
+        const size_t close = s_.find('>', i_);
+        if (close == std::string::npos) { err = "unterminated tag <" + n.name; return false; }
+        const bool empty = close > 0 && s_[close - 1] == '/';
+        i_ = close + 1;
+        if (empty) return true;
+        for (;;) {
+            if (i_ >= s_.size()) { err = "missing </" + n.name + ">"; return false; }
+            if (starts("<!--")) { if (!skip_past("-->")) { err = "unterminated comment"; return false; } continue; }
+            if (starts("<![CDATA[")) {
+                const size_t e = s_.find("]]>", i_);
+                if (e == std::string::npos) { err = "unterminated CDATA"; return false; }
+                n.text += s_.substr(i_ + 9, e - i_ - 9);
+                i_ = e + 3;
+                continue;
+            }
+            if (starts("</")) {
+                const size_t e = s_.find('>', i_);
+                if (e == std::string::npos) { err = "unterminated </" + n.name; return false; }
+                i_ = e + 1;
+                return true;
+            }
+            if (starts("<")) {
+                n.children.emplace_back();
+                if (!element(n.children.back(), err)) return false;
+                continue;
+            }
+            const size_t e = s_.find('<', i_);
+            std::string t = s_.substr(i_, (e == std::string::npos ? s_.size() : e) - i_);
+            decode(t);
+            n.text += t;
+            i_ = e == std::string::npos ? s_.size() : e;
+        }
+    }
+};
+
+inline std::vector<std::string> words(const std::string &t) {
+    std::istringstream in(t);
+    std::vector<std::string> w;
+    std::string x;
+    while (in >> x) w.push_back(x);
+    return w;
+}
+
+// "a b c" -> three numbers (the reference's Dim3::FromString: exactly three
+// whitespace-separated words, each read with std::stod)
+inline bool triple(const Node *n, double (&v)[3]) {
+    if (n == nullptr) return false;
+    const auto w = words(n->text);
+    if (w.size() != 3) return false;
+    try {
+        for (int k = 0; k < 3; ++k) v[k] = std::stod(w[k]);
+    } catch (const std::exception &) {
+        return false;
+    }
+    return true;
+}
+
+inline bool number(const Node *n, double &v) {
+    if (n == nullptr) return false;
+    try {
+        v = std::stod(n->text);
+    } catch (const std::exception &) {
+        return false;
+    }
+    return true;
+}
+
+}  // namespace kvxml
+
 class TomoGeometry {
 public:
+    // Reads a geometry file of the reference's format (TomoGeometry.cpp:13-434):
+    //   Rotation/center                     fulcrum (file frame)
+    //   Grid/center, Grid/scale, Grid/resolution   volume centre, voxel
+    //                                       spacing and voxel counts, each
+    //                                       written z y x
+    //   XRay/sources/*                      one source position per view
+    //   Camera/totalWidth, totalHeight      detector extent (mm)
+    //   Camera/pixelWidth, pixelHeight      detector pixel counts
+    //   Camera/references/*                 per-view detector bottom-left corner
+    //   Radios/rois/*                       the ROI, "x0 y0 . . x1 y1" pixels,
+    //                                       the same for every view
+    // Positions are moved to the volume-centred frame (minus Grid/center);
+    // the detector plane is the mean detector z (summed in double); the
+    // ROI's bottom-left position of view i is the detector corner plus the
+    // pixel pitch added pixel by pixel in float (TomoProjectionsSet.cpp:
+    // 172-190, 152-155), the pitch being extent / count (PixelSpacing.cpp).
+    explicit TomoGeometry(const std::string &xmlPath) { m_valid = read_xml(xmlPath); }
+
+private:
+    bool read_xml(const std::string &xmlPath) {
+        std::ifstream f(xmlPath, std::ios::binary);
+        if (!f) { m_error = "cannot open " + xmlPath; return false; }
+        std::stringstream ss;
+        ss << f.rdbuf();
+        const std::string src = ss.str();
+        kvxml::Node root;
+        std::string err;
+        if (!kvxml::Parser(src).parse(root, err)) { m_error = "XML: " + err; return false; }
+        auto fail = [this](const std::string &m) { m_error = m; return false; };
+        using kvxml::Node;
+        double v[3];
+        const Node *rot = root.child("Rotation");
+        if (!kvxml::triple(rot ? rot->child("center") : nullptr, v)) return fail("Rotation/center missing or unreadable");
+        m_fulcrum = {static_cast<float>(v[0]), static_cast<float>(v[1]), static_cast<float>(v[2])};
+        const Node *grid = root.child("Grid");
+        if (grid == nullptr) return fail("Grid missing");
+        double c[3], sc[3], res[3];
+        if (!kvxml::triple(grid->child("center"), c)) return fail("Grid/center missing or unreadable");
+        if (!kvxml::triple(grid->child("scale"), sc)) return fail("Grid/scale missing or unreadable");
+        if (!kvxml::triple(grid->child("resolution"), res)) return fail("Grid/resolution missing or unreadable");
+        const float cx = static_cast<float>(c[0]), cy = static_cast<float>(c[1]), cz = static_cast<float>(c[2]);
+        m_spacing = {static_cast<float>(sc[2]), static_cast<float>(sc[1]), static_cast<float>(sc[0])};
+        m_size = {static_cast<int>(static_cast<float>(res[2])), static_cast<int>(static_cast<float>(res[1])),
+                  static_cast<int>(static_cast<float>(res[0]))};
+        const Node *xr = root.child("XRay");
+        const Node *srcs = xr ? xr->child("sources") : nullptr;
+        if (srcs == nullptr || srcs->children.empty()) return fail("XRay/sources missing or empty");
+        std::vector<Position3D> sources;
+        for (const auto &sn : srcs->children) {
+            if (!kvxml::triple(&sn, v)) return fail("an XRay/sources entry is unreadable");
+            sources.push_back({static_cast<float>(v[0]) - cx, static_cast<float>(v[1]) - cy,
+                               static_cast<float>(v[2]) - cz});
+        }
+        const Node *cam = root.child("Camera");
+        if (cam == nullptr) return fail("Camera missing");
+        double tw, th, pw, ph;
+        if (!kvxml::number(cam->child("totalWidth"), tw) || static_cast<float>(tw) == 0.f)
+            return fail("Camera/totalWidth missing, unreadable or zero");
+        if (!kvxml::number(cam->child("totalHeight"), th) || static_cast<float>(th) == 0.f)
+            return fail("Camera/totalHeight missing, unreadable or zero");
+        if (!kvxml::number(cam->child("pixelWidth"), pw) || static_cast<float>(pw) == 0.f)
+            return fail("Camera/pixelWidth missing, unreadable or zero");
+        if (!kvxml::number(cam->child("pixelHeight"), ph) || static_cast<float>(ph) == 0.f)
+            return fail("Camera/pixelHeight missing, unreadable or zero");
+        const Size2D det_px{static_cast<int>(static_cast<float>(pw)), static_cast<int>(static_cast<float>(ph))};
+        if (det_px.x <= 0 || det_px.y <= 0) return fail("Camera pixel counts must be positive");
+        m_pixel = {static_cast<float>(tw) / static_cast<float>(det_px.x),
+                   static_cast<float>(th) / static_cast<float>(det_px.y)};
+        const Node *refs = cam->child("references");
+        if (refs == nullptr || refs->children.empty()) return fail("Camera/references missing or empty");
+        std::vector<Position2D> det_bl;
+        double zsum = 0.0;
+        for (const auto &rn : refs->children) {
+            if (!kvxml::triple(&rn, v)) return fail("a Camera/references entry is unreadable");
+            det_bl.push_back({static_cast<float>(v[0]) - cx, static_cast<float>(v[1]) - cy});
+            zsum += static_cast<float>(v[2]) - cz;
+        }
+        if (det_bl.size() != sources.size()) return fail("one detector reference per source is required");
+        m_detZ = static_cast<float>(zsum) / static_cast<float>(det_bl.size());
+        const Node *radios = root.child("Radios");
+        const Node *rois = radios ? radios->child("rois") : nullptr;
+        if (rois == nullptr || rois->children.empty()) return fail("Radios/rois missing or empty");
+        int bl[2] = {0, 0}, tr[2] = {0, 0};
+        for (size_t k = 0; k < rois->children.size(); ++k) {
+            const auto w = kvxml::words(rois->children[k].text);
+            if (w.size() < 6) return fail("a Radios/rois entry is unreadable");
+            int cur[4];
+            try {
+                cur[0] = static_cast<int>(std::stod(w[0]));
+                cur[1] = static_cast<int>(std::stod(w[1]));
+                cur[2] = static_cast<int>(std::stod(w[4]));
+                cur[3] = static_cast<int>(std::stod(w[5]));
+            } catch (const std::exception &) {
+                return fail("a Radios/rois entry is unreadable");
+            }
+            if (k == 0) {
+                bl[0] = cur[0]; bl[1] = cur[1]; tr[0] = cur[2]; tr[1] = cur[3];
+            } else if (bl[0] != cur[0] || bl[1] != cur[1] || tr[0] != cur[2] || tr[1] != cur[3]) {
+                return fail("the ROI differs between views");
+            }
+        }
+        auto clampi = [](int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); };
+        bl[0] = clampi(bl[0], 0, det_px.x - 1);
+        bl[1] = clampi(bl[1], 0, det_px.y - 1);
+        tr[0] = clampi(tr[0], 0, det_px.x - 1);
+        tr[1] = clampi(tr[1], 0, det_px.y - 1);
+        m_roiSize = {tr[0] - bl[0] + 1, tr[1] - bl[1] + 1};
+        for (const auto &d : det_bl) {
+            float x = d.x, y = d.y;
+            for (int k = 0; k < bl[0]; ++k) x += m_pixel.x;
+            for (int k = 0; k < bl[1]; ++k) y += m_pixel.y;
+            m_roiBL.push_back({x, y});
+        }
+        set_sources(sources);
+        return true;
+    }
+
+public:
+
     // volume: voxel counts and spacing, centred at the origin
     // sources: per-view positions (their x and z are averaged, as TomoTable
     //          does, TomoTable.cpp:4-19)
@@ -172,17 +430,11 @@ public:
           m_pixel(pixelSpacing), m_fulcrum(fulcrum), m_detZ(detectorZ) {
         if (sources.size() != roiBottomLeft.size() || sources.empty())
             throw std::invalid_argument("TomoGeometry: one source and one ROI origin per view");
-        float sx = 0.f, sz = 0.f;
-        for (const auto &s : sources) {
-            sx += s.x;
-            m_srcY.push_back(s.y);
-            sz += s.z;
-        }
-        m_srcX = sx / static_cast<float>(sources.size());
-        m_srcZ = sz / static_cast<float>(sources.size());
+        set_sources(sources);
         m_valid = true;
     }
     bool IsValid() const { return m_valid; }
+    const std::string &ErrorMessage() const { return m_error; }
 
     std::vector<float> sourcesYPositions() const { return m_srcY; }
     float sourcesXCommonPosition() const { return m_srcX; }
@@ -228,6 +480,19 @@ public:
     }
 
 private:
+    // common source x and z: float sums over the views (TomoTable.cpp:4-19)
+    void set_sources(const std::vector<Position3D> &sources) {
+        float sx = 0.f, sz = 0.f;
+        m_srcY.clear();
+        for (const auto &s : sources) {
+            sx += s.x;
+            m_srcY.push_back(s.y);
+            sz += s.z;
+        }
+        m_srcX = sx / static_cast<float>(sources.size());
+        m_srcZ = sz / static_cast<float>(sources.size());
+    }
+
     Size3D m_size;
     VoxelSpacing m_spacing;
     std::vector<float> m_srcY;
@@ -238,6 +503,7 @@ private:
     WSize3D m_fulcrum;
     float m_detZ = 0.f;
     bool m_valid = false;
+    std::string m_error;
 };
 
 // ---------------------------------------------------------------- engine

@@ -242,6 +242,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA issuer
         if (lane == 0) {
+            // descriptors of stage 0; a later stage, K step or sub-tile only adds
+            // its byte offset >> 4 to the start-address field (shared-memory
+            // addresses stay below 2^18, so the 14-bit field never carries)
+            uint64_t desc_a[kMaxSeg], desc_b[kMaxSeg];
+#pragma unroll
+            for (int s = 0; s < kMaxSeg; ++s) {
+                desc_a[s] = smem_desc(base + P.seg.a_off[s], (uint32_t)P.seg.kseg[s] * 2u);
+                desc_b[s] = smem_desc(base + P.seg.b_off[s], (uint32_t)P.seg.kseg[s] * 2u);
+            }
             uint32_t stage = 0, phase = 0, acc_phase = 0;
             for (long long tile = blockIdx.x; tile < P.tiles && !abort_flag; tile += gridDim.x) {
                 if (!mbar_wait(&acc_empty, acc_phase ^ 1u, &abort_flag, P.status, 2)) break;
@@ -251,17 +260,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int tap = 0; tap < 27 && ok; ++tap) {
                     if (!mbar_wait(&full_bar[stage], phase, &abort_flag, P.status, 3)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t sb = base + stage * P.stage_bytes;
-                    for (int s = 0; s < P.seg.n; ++s) {
-                        const uint32_t rb = (uint32_t)P.seg.kseg[s] * 2u;      // row bytes of this segment
+                    const uint64_t so = (uint64_t)((stage * P.stage_bytes) >> 4);
+#pragma unroll
+                    for (int s = 0; s < kMaxSeg; ++s) {
+                        if (s >= P.seg.n) break;
+                        const uint64_t sub = (uint64_t)((kTileM * P.seg.kseg[s] * 2) >> 4);   // one sub-tile
                         for (int k = 0; k < P.seg.kseg[s]; k += 16) {
-                            const uint64_t bd = smem_desc(sb + P.seg.b_off[s] + (uint32_t)k * 2u, rb);
-                            for (int j = 0; j < P.T; ++j) {   // sub-tile j: rows 128j.., TMEM columns jN..
-                                const uint64_t ad =
-                                    smem_desc(sb + P.seg.a_off[s] + (uint32_t)j * kTileM * rb + (uint32_t)k * 2u, rb);
-                                tc_mma(tmem + (uint32_t)(j * P.N), ad, bd, P.idesc,
-                                       (tap > 0 || s > 0 || k > 0) ? 1u : 0u);
-                            }
+                            const uint64_t ko = (uint64_t)((k * 2) >> 4);                   // 32 B per K step
+                            const uint64_t bd = desc_b[s] + so + ko;
+                            for (int j = 0; j < P.T; ++j)   // sub-tile j: rows 128j.., TMEM columns jN..
+                                tc_mma(tmem + (uint32_t)(j * P.N), desc_a[s] + so + ko + (uint64_t)j * sub, bd,
+                                       P.idesc, (tap > 0 || s > 0 || k > 0) ? 1u : 0u);
                         }
                     }
                     tc_commit(&empty_bar[stage]);      // frees the stage when these MMAs are done

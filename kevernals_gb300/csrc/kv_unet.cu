@@ -414,7 +414,7 @@ kv_status conv3(kv_unet *u, int layer, const bf16 *in1, const bf16 *in2, bf16 *o
     const int blocks = (int)((nvox / 16 + 3) / 4);
     LaunchTimer lt(ctx, weights_t ? "unet_conv_dgrad" : "unet_conv_fwd");
     int bw, bh, bd;
-    if (c1 + c2 >= 32 && cout >= 32 && convtc::tile_shape(D, H, W, bw, bh, bd)) {
+    if (convtc::tile_shape(D, H, W, bw, bh, bd)) {
         // tcgen05 / TMA implicit GEMM (kv_conv_tc.cuh)
         const char *why = convtc::launch(in1, c1, in2, c2, w, bias, !weights_t, out, cout, D, H, W, u->tc_status,
                                          ctx->sm_count, ctx->stream);
@@ -422,9 +422,8 @@ kv_status conv3(kv_unet *u, int layer, const bf16 *in1, const bf16 *in2, bf16 *o
         KV_CHECK_LAUNCH(ctx, "unet conv3 (tcgen05)");
         return KV_OK;
     }
-    // 16-channel convolutions, and volumes smaller than one 128-voxel tile:
-    // warp-level mma.sync (a 128 x 16 x 16 tcgen05 MMA per tap is too little
-    // work per TMA load to pay)
+    // volumes that are not a whole number of 128-voxel tiles (the deepest
+    // levels of small inputs): warp-level mma.sync
     for (int n0 = 0; n0 < cout; n0 += 64) {
         const int nc = cout - n0 < 64 ? cout - n0 : 64;
         const bool relu = !weights_t;

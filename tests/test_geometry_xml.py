@@ -1,0 +1,119 @@
+"""The drop-in header's reader of the reference's XML geometry files
+(TomoGeometry(path), source/modules/geometry/TomoGeometry.cpp:13-434), on
+the host: a synthetic file in that schema is read and its flattened
+description is compared with the derivation restated here in float32
+(TomoTable.cpp:4-19, TomoProjectionsSet.cpp:152-190, PixelSpacing.cpp,
+Projector.cu:917-940).  The reference ships no geometry files, so this
+reader's parity is pinned by the restated derivation only."""
+import json
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+f32 = np.float32
+
+
+def write_xml(path, centre=(10.0, 20.0, 40.0), res=(16, 64, 48), scale=(1.0, 0.5, 0.5), views=5,
+              roi="10 20 0 0 89 79", rois=None, drop=None):
+    cx, cy, cz = centre
+    ys = np.linspace(-150.0, 150.0, views)
+    parts = ['<?xml version="1.0" encoding="UTF-8"?>', "<!-- synthetic linear-sweep geometry -->", "<Geometry>"]
+    if drop != "Rotation":
+        parts.append(f"  <Rotation><center>{cx} {cy} {cz + 150.0}</center></Rotation>")
+    if drop != "Grid":
+        parts.append(f"  <Grid><center>{cx} {cy} {cz}</center><scale>{scale[0]} {scale[1]} {scale[2]}</scale>"
+                     f"<resolution>{res[0]} {res[1]} {res[2]}</resolution></Grid>")
+    parts.append("  <XRay><sources>")
+    for i, y in enumerate(ys):
+        parts.append(f"    <source>{cx + 0.25 * i} {cy + y} {cz + 900.0 + 0.1 * i}</source>")
+    parts.append("  </sources></XRay>")
+    parts.append("  <Camera><totalWidth>40</totalWidth><totalHeight>30</totalHeight>"
+                 "<pixelWidth>100</pixelWidth><pixelHeight>75</pixelHeight><references>")
+    for i in range(views):
+        parts.append(f"    <reference>{cx - 20.0 + 0.01 * i} {cy - 15.0} {cz - 60.0 + 0.001 * i}</reference>")
+    parts.append("  </references></Camera>")
+    parts.append("  <Radios><rois>")
+    for i in range(views):
+        parts.append(f"    <roi>{rois[i] if rois else roi}</roi>")
+    parts.append("  </rois></Radios>")
+    parts.append("</Geometry>")
+    with open(path, "w") as fh:
+        fh.write("\n".join(parts) + "\n")
+
+
+@pytest.fixture(scope="module")
+def dumper(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path_factory.mktemp("xml") / "geometry_xml_dump")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "geometry_xml_dump.cpp"), "-o", exe], check=True)
+    return exe
+
+
+def read(dumper, path):
+    out = subprocess.run([dumper, path], check=True, capture_output=True, text=True).stdout
+    return json.loads(out)
+
+
+def expected(centre, res, scale, views, roi_bl, roi_tr):
+    cx, cy, cz = (f32(c) for c in centre)
+    ys = np.linspace(-150.0, 150.0, views)
+    src = [(f32(cx + 0.25 * i) - cx, f32(cy + y) - cy, f32(cz + 900.0 + 0.1 * i) - cz) for i, y in enumerate(ys)]
+    sx = f32(0)
+    sz = f32(0)
+    for s in src:
+        sx = f32(sx + s[0])
+        sz = f32(sz + s[2])
+    sx = f32(sx / f32(views))
+    sz = f32(sz / f32(views))
+    det_bl = [(f32(cx - 20.0 + 0.01 * i) - cx, f32(cy - 15.0) - cy) for i in range(views)]
+    zsum = 0.0
+    for i in range(views):
+        zsum += float(f32(cz - 60.0 + 0.001 * i) - cz)
+    detz = f32(f32(zsum) / f32(views))
+    du, dv = f32(f32(40) / f32(100)), f32(f32(30) / f32(75))
+    det = []
+    for x, y in det_bl:
+        for _ in range(roi_bl[0]):
+            x = f32(x + du)
+        for _ in range(roi_bl[1]):
+            y = f32(y + dv)
+        det.append((x, y, detz))
+    return {"n": [res[2], res[1], res[0]], "d": [scale[2], scale[1], scale[0]], "views": views,
+            "det": [roi_tr[0] - roi_bl[0] + 1, roi_tr[1] - roi_bl[1] + 1], "pitch": [du, dv],
+            "fulcrum_z": f32(centre[2] + 150.0),   # Rotation/center stays in the file's frame
+            "src": [v for s in src for v in (sx, f32(s[1]), sz)], "det_origin": [v for d in det for v in d]}
+
+
+def test_xml_geometry_matches_restated_derivation(dumper, tmp_path):
+    path = str(tmp_path / "geo.xml")
+    write_xml(path)
+    got = read(dumper, path)
+    assert got["valid"], got
+    # the ROI's top row 79 is clamped to the detector's last row, 74
+    exp = expected((10.0, 20.0, 40.0), (16, 64, 48), (1.0, 0.5, 0.5), 5, (10, 20), (89, 74))
+    assert got["n"] == exp["n"] and got["views"] == exp["views"] and got["det"] == exp["det"]
+    for k in ("d", "pitch", "src", "det_origin"):
+        assert np.array_equal(np.asarray(got[k], np.float32), np.asarray(exp[k], np.float32)), k
+    assert np.float32(got["fulcrum_z"]) == exp["fulcrum_z"]
+
+
+def test_xml_geometry_rejects_bad_files(dumper, tmp_path):
+    path = str(tmp_path / "bad.xml")
+    write_xml(path, drop="Grid")
+    got = read(dumper, path)
+    assert not got["valid"] and "Grid" in got["error"]
+    write_xml(path, rois=["10 20 0 0 89 79"] * 2 + ["11 20 0 0 89 79"] + ["10 20 0 0 89 79"] * 2)
+    got = read(dumper, path)
+    assert not got["valid"] and "ROI" in got["error"]
+    with open(path, "w") as fh:
+        fh.write("<Geometry><Grid><center>1 2 3</center>")
+    got = read(dumper, path)
+    assert not got["valid"] and "XML" in got["error"]
+    got = read(dumper, str(tmp_path / "missing.xml"))
+    assert not got["valid"] and "cannot open" in got["error"]
