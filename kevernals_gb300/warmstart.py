@@ -152,9 +152,29 @@ def window_offset(seed, crop: Geometry):
     return [rng.uniform(-0.8 * r, 0.8 * r) if r > 0 else 0.0 for r in room]
 
 
-def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100, params=None):
+# A voxel is "seen" when its sensitivity (A^T 1) is at least this fraction of
+# the median over voxels that some ray crosses.  At the chest-DT geometry the
+# cone misses the lateral edges of the upper slices: MLEM never updates those
+# voxels (they keep the start value), and voxels crossed by only a few views
+# are barely constrained, so neither carries a usable training target.
+SEEN_FRACTION = 0.1
+
+
+def seen_mask(plan):
+    """Boolean volume: voxels whose sensitivity reaches SEEN_FRACTION of the
+    median sensitivity of the voxels crossed by any ray."""
+    sens = plan.sensitivity(device=True)
+    pos = sens[sens > 0]
+    if pos.numel() == 0:
+        return sens > 0
+    thr = SEEN_FRACTION * float(pos.float().median())
+    return sens >= thr
+
+
+def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100, params=None, mask_unseen=False):
     """(shift-and-add, MLEM target, data) for one seeded phantom, on the GPU;
-    `params` (ellipsoid rows) overrides the phantom drawn for g."""
+    `params` (ellipsoid rows) overrides the phantom drawn for g.  With
+    mask_unseen the target is NaN (no training target) outside seen_mask()."""
     import torch
     if params is None:
         params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ellipsoids, seed)
@@ -164,6 +184,8 @@ def make_triple(ctx, g, seed, n_ellipsoids=40, i0=5e4, target_iters=100, params=
     s = shift_and_add_volume(plan, p)
     x = torch.ones(g.volume_shape, dtype=torch.float32, device=p.device)
     plan.mlem(p, x, target_iters)
+    if mask_unseen:
+        x[~seen_mask(plan)] = float("nan")
     torch.cuda.synchronize()
     plan.close()
     return s, x, p
@@ -189,6 +211,10 @@ def warm_start(plan, net, p):
     import torch
     s = shift_and_add_volume(plan, p)
     x0 = net.forward(s).clamp_(min=EPS)
+    # voxels outside the network's training support (unseen or barely seen
+    # by the rays) start from the shift-and-add value
+    unseen = ~seen_mask(plan)
+    x0[unseen] = s[unseen].clamp(min=EPS)
     ones = torch.ones_like(x0)
     r_w, _ = plan.residual(p, x0)
     r_u, _ = plan.residual(p, ones)
@@ -296,7 +322,8 @@ def _cli():
             params = None
             if args.phantom == "chest":
                 gc = config_chest()
-                s, x, _ = make_triple(ctx, gc, seed, n_ellipsoids=400, target_iters=args.target_iters)
+                s, x, _ = make_triple(ctx, gc, seed, n_ellipsoids=400, target_iters=args.target_iters,
+                                      mask_unseen=True)
                 triples.extend(chest_crops(s, x, nx, ny, args.crops_per_volume, seed))
                 del s, x
                 if (i + 1) % 4 == 0:
