@@ -302,6 +302,10 @@ def _cli():
                          "columns of chest-DT phantoms seen by the chest geometry's own rays, windows of "
                          "chest-DT phantoms in the centred crop geometry, or phantoms drawn for the crop")
     ap.add_argument("--crops-per-volume", type=int, default=16)
+    ap.add_argument("--init", default=None,
+                    help="start training from this checkpoint (full state or weights only)")
+    ap.add_argument("--first-case", type=int, default=0,
+                    help="seed index of the first training phantom (continue with fresh phantoms)")
     args = ap.parse_args()
     import torch
     os.makedirs(args.out, exist_ok=True)
@@ -317,7 +321,9 @@ def _cli():
         g = crop_geometry(nx, ny, nz)
         t0 = time.perf_counter()
         triples = []
-        for i in range(args.triples):
+        if args.init:
+            net.load(args.init)
+        for i in range(args.first_case, args.first_case + args.triples):
             seed = ph.seed_for(5, i)
             params = None
             if args.phantom == "chest":
@@ -326,8 +332,8 @@ def _cli():
                                       mask_unseen=True)
                 triples.extend(chest_crops(s, x, nx, ny, args.crops_per_volume, seed))
                 del s, x
-                if (i + 1) % 4 == 0:
-                    log(f"{i + 1} chest triples, {time.perf_counter() - t0:.1f} s")
+                if (i + 1 - args.first_case) % 4 == 0:
+                    log(f"{i + 1 - args.first_case} chest triples, {time.perf_counter() - t0:.1f} s")
                 continue
             if args.phantom == "column":
                 g, centre = column_geometry(column_centre(seed, nx, ny), nx, ny)
@@ -364,7 +370,8 @@ def _cli():
         hist = train(net, triples, args.epochs, args.lr, log=log, on_epoch=on_epoch)
         t_train = time.perf_counter() - t0
         report = {"triples": len(triples), "crop": [nx, ny, nz], "target_iters": args.target_iters,
-                  "phantom": args.phantom, "volumes": args.triples,
+                  "phantom": args.phantom, "volumes": args.triples, "first_case": args.first_case,
+                  "init": args.init,
                   "epochs": args.epochs, "lr": args.lr, "generate_s": t_gen, "train_s": t_train,
                   "loss_history": hist, "held_out_mse": val_hist, "checkpoint": path}
     else:
