@@ -409,16 +409,18 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
                "h2d_bytes_per_step": 4 * (g.n_rays + g.n_voxels), "d2h_bytes_per_step": 4 * g.n_voxels,
                "ms_per_step": ems / args.steps}
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline_exact(g, truth.cpu().numpy(), p.cpu().numpy(), args.cpu_seconds)
-    ref_gpu_line = reference_gpu(g, truth) if rank == 0 and not args.no_ref_gpu else None
+    # the learned-warm-start comparison runs before the CPU and reference
+    # legs, on a GPU and host that nothing else is using
     ttr = None
     if (not args.no_ttr and args.workload == "chest" and args.family == "exact"
             and args.storage == "f32" and args.views == 0):
         del x
         plan.close()
         ttr = time_to_residual(ctx, g, cfg, rank)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline_exact(g, truth.cpu().numpy(), p.cpu().numpy(), args.cpu_seconds)
+    ref_gpu_line = reference_gpu(g, truth) if rank == 0 and not args.no_ref_gpu else None
 
     if rank == 0:
         out = {

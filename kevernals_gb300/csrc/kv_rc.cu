@@ -113,29 +113,40 @@ __global__ void __launch_bounds__(128) rc_forward_kernel(RcGeom G, const float *
             }
         }
         int ones = total - filled;   // entries left at the fill value 1.0
-        const float base[3] = {half[0] + s[0], half[1] + s[1], half[2] + s[2]};
+        const float b0 = half[0] + s[0], b1 = half[1] + s[1], b2 = half[2] + s[2];
+        const float d0 = d[0], d1 = d[1], d2 = d[2];
+        // the three sequences as scalars (a dynamically indexed array would
+        // live in local memory and every merge step would go through L1)
+        float v0 = sq[0].val, v1 = sq[1].val, v2 = sq[2].val;
+        const float st0 = sq[0].step, st1 = sq[1].step, st2 = sq[2].step;
+        int l0 = sq[0].left, l1 = sq[1].left, l2 = sq[2].left;
         float acc = 0.F, wsum = 0.F;
         float prev = 0.F;
         for (int e = 0; e < total; ++e) {
             // pop the smallest head among x, y, z and the 1.0 entries
             float best = 3.402823466e38F;
             int which = 3;
-            if (sq[0].left > 0) { best = sq[0].val; which = 0; }
-            if (sq[1].left > 0 && sq[1].val < best) { best = sq[1].val; which = 1; }
-            if (sq[2].left > 0 && sq[2].val < best) { best = sq[2].val; which = 2; }
+            if (l0 > 0) { best = v0; which = 0; }
+            if (l1 > 0 && v1 < best) { best = v1; which = 1; }
+            if (l2 > 0 && v2 < best) { best = v2; which = 2; }
             if (ones > 0 && 1.0F < best) { best = 1.0F; which = 3; }
-            if (which == 3) {
-                if (ones > 0) --ones;
-            } else {
-                Seq &z = sq[which];
-                z.val = z.val + z.step;
-                --z.left;
+            if (which == 0) {
+                v0 = v0 + st0;
+                --l0;
+            } else if (which == 1) {
+                v1 = v1 + st1;
+                --l1;
+            } else if (which == 2) {
+                v2 = v2 + st2;
+                --l2;
+            } else if (ones > 0) {
+                --ones;
             }
             if (e > 0) {
                 const float c = (best + prev) * 0.5F;
-                const int ix = rc_index(base[0], c, d[0]);
-                const int iy = rc_index(base[1], c, d[1]);
-                const int iz = rc_index(base[2], c, d[2]);
+                const int ix = rc_index(b0, c, d0);
+                const int iy = rc_index(b1, c, d1);
+                const int iz = rc_index(b2, c, d2);
                 const float w = best - prev;
                 if (ix >= 0 && ix < G.nx && iy >= 0 && iy < G.ny && iz >= 0 && iz < G.nz && w > tol) {
                     const size_t idx = ((size_t)iz * G.ny + iy) * G.nx + ix;
