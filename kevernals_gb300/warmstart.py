@@ -271,6 +271,19 @@ def iterations_to_residual(plan, p, x, target, max_iters, reject_above=None):
     return state["n"], state["r"]
 
 
+def _start_estimate(plan, net, p):
+    """The network's start (blind spots filled from the shift-and-add volume)
+    and the uniform start's residual from the prepared A1."""
+    c = prepare(plan)
+    s = shift_and_add_volume(plan, p)
+    x0 = net.forward(s).clamp_(min=EPS)
+    unseen = ~c["seen"]
+    x0[unseen] = s[unseen].clamp(min=EPS)
+    pd = p.double()
+    r_u = float((c["a1"].double() - pd).norm() / pd.norm())
+    return x0, r_u
+
+
 def warm_start_mlem(plan, net, p, target, max_iters):
     """The learned warm start followed by MLEM until the residual reaches
     `target`.  The network's estimate is kept only if its data residual is
@@ -280,13 +293,7 @@ def warm_start_mlem(plan, net, p, target, max_iters):
     rejected estimate falls back to MLEM from the uniform start.
     Returns (x, iterations, residual, accepted, start_residual, uniform_residual)."""
     import torch
-    c = prepare(plan)
-    s = shift_and_add_volume(plan, p)
-    x0 = net.forward(s).clamp_(min=EPS)
-    unseen = ~c["seen"]
-    x0[unseen] = s[unseen].clamp(min=EPS)
-    pd = p.double()
-    r_u = float((c["a1"].double() - pd).norm() / pd.norm())
+    x0, r_u = _start_estimate(plan, net, p)
     n, r, r_start, rejected = iterations_to_residual(plan, p, x0, target, max_iters, reject_above=r_u)
     if rejected:
         x0 = torch.ones_like(x0)
@@ -306,9 +313,11 @@ def evaluate_case(ctx, net, g, seed, plain_iters=50, tol=0.01, i0=5e4, n_ellipso
     plan = engine.Plan(ctx, g, "exact")
     p = noisy_data(ctx, plan, truth, i0, seed)
     # one-time set-up, outside both timings: per geometry A1, the sensitivity
-    # image and the seen mask; per volume shape the network's workspace
+    # image and the seen mask; per volume shape the network's workspace; per
+    # process the first use of the elementwise tensor operations of the start
+    # (a fresh process loads / compiles them on first use, which took ~3 s)
     prepare(plan)
-    net.forward(torch.zeros(g.volume_shape, dtype=torch.float32, device="cuda"))
+    _start_estimate(plan, net, p)
     torch.cuda.synchronize()
     # plain MLEM
     x = torch.ones(g.volume_shape, dtype=torch.float32, device="cuda")
