@@ -143,6 +143,17 @@ kv_status kv_sensitivity(kv_plan *plan, double *sens, kv_mem mem);
  * literally (Reconstructors.h:308-331); EXACT measures heights from the
  * detector plane and shifts in detector pixels. */
 kv_status kv_shift_and_add(kv_plan *plan, const float *projections, float *slices, kv_mem mem);
+/* Filtered backprojection for tomosynthesis (EXACT family, FP32 storage):
+ *   volume = A^T(h * p) / A^T 1   (0 where A^T 1 = 0)
+ * where h * p filters every detector column along v, the tube's sweep
+ * direction, with the Shepp-Logan ramp kernel h[n] = -2 / (pi^2 (4n^2 - 1))
+ * (pixel units) truncated at |n| <= half_taps (1..KV_FBP_MAX_HALF_TAPS),
+ * zero outside the detector.  A sharpened shift-and-add: the same
+ * normalisation as one SART step from zero, with ramp-filtered data.  The
+ * reference's "FBP" reconstructor is an unfiltered backprojection
+ * (backup/TomosynthesisFBPReconstructor.cpp); this is the filtered method. */
+#define KV_FBP_MAX_HALF_TAPS 256
+kv_status kv_fbp(kv_plan *plan, const float *projections, float *volume, int32_t half_taps, kv_mem mem);
 /* Host-only: the integer row shift of every (slice, view) pair that
  * kv_shift_and_add applies, [nz][n_views], computed without a device.
  * Replaces the shift loop of recons::ShiftAndAdd, Reconstructors.h:308-331. */

@@ -53,6 +53,7 @@ SIGNATURES = {
     "kv_back": ([_vp, _vp, _vp, C.c_int], C.c_int),
     "kv_sensitivity": ([_vp, _vp, C.c_int], C.c_int),
     "kv_shift_and_add": ([_vp, _vp, _vp, C.c_int], C.c_int),
+    "kv_fbp": ([_vp, _vp, _vp, C.c_int32, C.c_int], C.c_int),
     "kv_shift_and_add_shifts": ([C.POINTER(KvGeometry), C.c_int, _vp], C.c_int),
     "kv_uniform_volume": ([_vp, _vp, C.c_int], C.c_int),
     "kv_phantom_ellipsoids": ([_vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float,

@@ -452,6 +452,30 @@ extern "C" kv_status kv_back(kv_plan *plan, const float *proj, float *volume, kv
     return stage_out(plan, volume, mem, vd, plan->nvox);
 }
 
+extern "C" kv_status kv_fbp(kv_plan *plan, const float *proj, float *volume, int32_t half_taps, kv_mem mem) {
+    KV_TRY(check_common(plan, proj, volume, mem));
+    if (plan->family != KV_FAMILY_EXACT || plan->storage != KV_STORAGE_F32)
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "filtered backprojection needs the EXACT family, FP32 storage");
+    if (half_taps < 1 || half_taps > KV_FBP_MAX_HALF_TAPS)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "half_taps must be 1..%d (got %d)", KV_FBP_MAX_HALF_TAPS,
+                       half_taps);
+    float *pd, *vd;
+    KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
+    KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, false, &vd));
+    KV_TRY(ensure_sens(plan));
+    KV_TRY(ensure(plan->ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
+    float *filtered = nullptr;
+    KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&filtered, plan->nproj * sizeof(float), plan->ctx->stream));
+    kv_status st = ramp_filter_launch(plan, pd, filtered, half_taps);
+    if (st == KV_OK) st = exact_prescale_launch(plan, filtered, plan->d_ratio);
+    cudaFreeAsync(filtered, plan->ctx->stream);
+    KV_TRY(st);
+    // volume = 0 + 1 * A^T(y) / A^T 1: the SART-mode update epilogue from zero
+    KV_TRY(fill_launch(plan->ctx, vd, plan->nvox, 0.f));
+    KV_TRY(exact_back_launch(plan, BACK_SART, BackArgs{plan->d_ratio, vd, plan->d_sens, 1.f}));
+    return stage_out(plan, volume, mem, vd, plan->nvox);
+}
+
 extern "C" kv_status kv_sensitivity(kv_plan *plan, double *sens, kv_mem mem) {
     if (plan == nullptr) return KV_ERR_INVALID_ARG;
     if (sens == nullptr) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "null buffer");

@@ -219,6 +219,7 @@ kv_status rc_forward_launch(kv_plan *plan, const float *d_src, const float *d_or
 kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol);
 
 kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out);
+kv_status ramp_filter_launch(kv_plan *plan, const float *in, float *out, int half_taps);
 kv_status fill_launch(kv_ctx *ctx, float *p, size_t n, float v);
 kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_storage s);
 kv_status convert_back_launch(kv_ctx *ctx, const void *in, float *out, size_t n, kv_storage s);

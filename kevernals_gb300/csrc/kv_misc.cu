@@ -1,6 +1,8 @@
 // kv_misc.cu -- shift-and-add, phantom rasteriser and elementwise kernels.
 #include "kv_internal.h"
 
+#include <cmath>
+
 namespace {
 
 // Shift-and-add (recons::ShiftAndAdd, Reconstructors.h:263-379):
@@ -155,6 +157,63 @@ int grid_for(const kv_ctx *ctx, size_t n, int block) {
 }
 
 }  // namespace
+
+// Ramp filtering of the projections along v (the tube's sweep direction)
+// for the filtered backprojection: out[p][v][u] = sum_{|k|<=K} h[|k|] *
+// in[p][v-k][u], zero outside the detector.  h is the Shepp-Logan kernel
+// h[n] = -2 / (pi^2 (4 n^2 - 1)) in pixel units (L. A. Shepp, B. F. Logan,
+// IEEE Trans. Nucl. Sci. 21, 1974), truncated at |n| <= K and passed by
+// value.  A block holds 32 columns and 32 output rows; the 32 + 2K input
+// rows it needs are staged in shared memory (zeros outside the detector),
+// and each thread sums the symmetric taps pairwise in FP32.
+namespace {
+
+struct RampTaps {
+    float h[KV_FBP_MAX_HALF_TAPS + 1];
+};
+
+constexpr int kRampRows = 32;
+
+__global__ void __launch_bounds__(256) ramp_v_kernel(const float *__restrict__ in, float *__restrict__ out, int nu,
+                                                     int nv, int K, const RampTaps taps) {
+    extern __shared__ float tile[];   // [kRampRows + 2K][32]
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int u = blockIdx.x * 32 + tx;
+    const int v0 = blockIdx.y * kRampRows;
+    const size_t base = (size_t)blockIdx.z * nv * nu;
+    const int rows = kRampRows + 2 * K;
+    for (int r = ty; r < rows; r += blockDim.y) {
+        const int v = v0 - K + r;
+        tile[r * 32 + tx] = (u < nu && v >= 0 && v < nv) ? __ldg(in + base + (size_t)v * nu + u) : 0.f;
+    }
+    __syncthreads();
+    if (u >= nu) return;
+    for (int o = ty; o < kRampRows; o += blockDim.y) {
+        const int v = v0 + o;
+        if (v >= nv) break;
+        const float *c = tile + (o + K) * 32 + tx;     // input row v
+        float acc = taps.h[0] * c[0];
+        for (int k = 1; k <= K; ++k) acc = fmaf(taps.h[k], c[-k * 32] + c[k * 32], acc);
+        out[base + (size_t)v * nu + u] = acc;
+    }
+}
+
+}  // namespace
+
+kv_status ramp_filter_launch(kv_plan *plan, const float *in, float *out, int half_taps) {
+    const kv_geometry &g = plan->g;
+    RampTaps taps;
+    for (int n = 0; n <= half_taps; ++n)
+        taps.h[n] = (float)(-2.0 / (M_PI * M_PI * (4.0 * (double)n * n - 1.0)));
+    const size_t smem = (size_t)(kRampRows + 2 * half_taps) * 32 * sizeof(float);
+    KV_CHECK_CUDA(plan->ctx, cudaFuncSetAttribute(ramp_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)smem));
+    dim3 block(32, 8), grid((g.nu + 31) / 32, (g.nv + kRampRows - 1) / kRampRows, g.n_views);
+    LaunchTimer lt(plan->ctx, "ramp_v");
+    ramp_v_kernel<<<grid, block, smem, plan->ctx->stream>>>(in, out, g.nu, g.nv, half_taps, taps);
+    KV_CHECK_LAUNCH(plan->ctx, "ramp_v_kernel");
+    return KV_OK;
+}
 
 kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out) {
     const kv_geometry &g = plan->g;

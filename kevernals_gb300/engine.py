@@ -203,6 +203,18 @@ class Plan:
         self.ctx.check(lib().kv_back(self._h, pp, po, mp))
         return out
 
+    def fbp(self, proj, half_taps=128, out=None):
+        """Filtered backprojection: A^T(h * p) / A^T 1 with the Shepp-Logan
+        ramp along v truncated at |n| <= half_taps (kv_fbp)."""
+        g = self.geometry
+        out = self._like(proj, g.volume_shape) if out is None else out
+        pp, mp, kp = self._buf(proj, g.proj_shape)
+        po, mo, ko = self._buf(out, g.volume_shape, out=True)
+        if mp != mo:
+            raise ValueError("input and output must both be host or both be device buffers")
+        self.ctx.check(lib().kv_fbp(self._h, pp, po, int(half_taps), mp))
+        return out
+
     def sensitivity(self, out=None, device=False):
         g = self.geometry
         if out is None:

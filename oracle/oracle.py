@@ -255,3 +255,30 @@ def ref_back(g, proj):
     out = np.empty(g.volume_shape, np.float32)
     L.kvref_back(C.byref(cgeom(g)), _proj(g, proj, np.float32), out)
     return out
+
+
+def ramp_taps(half_taps):
+    """Shepp-Logan ramp kernel in pixel units, h[n] = -2 / (pi^2 (4n^2 - 1)),
+    n = 0..half_taps (L. A. Shepp, B. F. Logan, IEEE Trans. Nucl. Sci. 21, 1974)."""
+    n = np.arange(half_taps + 1, dtype=np.float64)
+    return -2.0 / (np.pi ** 2 * (4.0 * n * n - 1.0))
+
+
+def ramp_filter_v(proj, half_taps):
+    """FP64 filtering of every detector column along v with the truncated
+    Shepp-Logan kernel, zero outside the detector ([P][nv][nu] layout)."""
+    p = np.asarray(proj, np.float64)
+    h = ramp_taps(half_taps)
+    out = h[0] * p
+    nv = p.shape[1]
+    for k in range(1, min(half_taps, nv - 1) + 1):
+        out[:, k:, :] += h[k] * p[:, :-k, :]
+        out[:, :-k, :] += h[k] * p[:, k:, :]
+    return out
+
+
+def exact_fbp(g, proj, half_taps):
+    """A^T(h * p) / A^T 1 (0 where A^T 1 = 0), the engine's kv_fbp, in FP64."""
+    b = exact_back(g, ramp_filter_v(proj, half_taps))
+    s = exact_back(g, np.ones(g.proj_shape))
+    return np.where(s > 0, b / np.where(s > 0, s, 1.0), 0.0)

@@ -150,6 +150,28 @@ def test_exact_dot_product(ctx, gi):
     assert abs(lhs - rhs) <= DOT_REL * abs(lhs)
 
 
+@pytest.mark.parametrize("gi,half_taps", [(0, 8), (2, 64)])
+def test_exact_fbp_vs_fp64_oracle(ctx, gi, half_taps):
+    """Filtered backprojection (Shepp-Logan ramp along v, then A^T and the
+    sensitivity normalisation) against its FP64 restatement."""
+    g = small_geoms()[gi]
+    vol = phantom_for(g)
+    plan = engine.Plan(ctx, g, "exact")
+    p = plan.forward(vol)
+    x = plan.fbp(p, half_taps)
+    ref = O.exact_fbp(g, p, half_taps)
+    assert rel_l2(x, ref) < 1e-5
+    # the ramp sharpens: closer to the phantom than the plain normalised backprojection
+    sens = O.exact_back(g, np.ones(g.proj_shape))
+    saa = np.where(sens > 0, O.exact_back(g, p) / np.where(sens > 0, sens, 1.0), 0.0)
+    if half_taps >= 16:
+        assert rel_l2(x, vol) < rel_l2(saa, vol)
+    with pytest.raises(KvError):
+        plan.fbp(p, 0)
+    with pytest.raises(KvError):
+        plan.fbp(p, 257)
+
+
 def test_exact_sensitivity_vs_oracle(ctx):
     g = small_geoms()[0]
     plan = engine.Plan(ctx, g, "exact")
