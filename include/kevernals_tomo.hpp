@@ -96,20 +96,23 @@ inline std::error_code make_error_code(ReconstructorsErrorCode e) {
 }
 
 // Value-or-error, the subset of outcome::result the reference uses.
+// The error state is kept apart from the code's value: an enumerator whose
+// value is 0 (DICOMReaderErrorCode::DataFileReadingProblem) is still an
+// error, as in outcome::result.
 template <typename T> class Result {
 public:
     Result(T v) : m_value(std::move(v)) {}
-    Result(std::error_code e) : m_error(e) {}
-    Result(ReconstructorsErrorCode e) : m_error(make_error_code(e)) {}
-    bool has_value() const { return !m_error; }
-    bool has_error() const { return static_cast<bool>(m_error); }
+    Result(std::error_code e) : m_error(e), m_failed(true) {}
+    Result(ReconstructorsErrorCode e) : m_error(make_error_code(e)), m_failed(true) {}
+    bool has_value() const { return !m_failed; }
+    bool has_error() const { return m_failed; }
     explicit operator bool() const { return has_value(); }
     const T &value() const {
-        if (m_error) throw std::system_error(m_error);
+        if (m_failed) throw std::system_error(m_error);
         return m_value;
     }
     T &value() {
-        if (m_error) throw std::system_error(m_error);
+        if (m_failed) throw std::system_error(m_error);
         return m_value;
     }
     std::error_code error() const { return m_error; }
@@ -117,6 +120,7 @@ public:
 private:
     T m_value{};
     std::error_code m_error{};
+    bool m_failed = false;
 };
 
 // ---------------------------------------------------------------- images
@@ -406,6 +410,7 @@ private:
         tr[0] = clampi(tr[0], 0, det_px.x - 1);
         tr[1] = clampi(tr[1], 0, det_px.y - 1);
         m_roiSize = {tr[0] - bl[0] + 1, tr[1] - bl[1] + 1};
+        m_roiBLPixel = {bl[0], bl[1]};
         for (const auto &d : det_bl) {
             float x = d.x, y = d.y;
             for (int k = 0; k < bl[0]; ++k) x += m_pixel.x;
@@ -445,6 +450,11 @@ public:
     int nbProjectionsRois() const { return nbProjections(); }
     std::vector<Position2D> projectionsRoisBottomLeftPositions() const { return m_roiBL; }
     Size2D projectionsRoisSize() const { return m_roiSize; }
+    // The ROI's bottom-left pixel on the full detector (TomoGeometry.h, used
+    // by DICOMReader to crop the raw images); {0, 0} unless read from a
+    // geometry file or set.
+    Size2D GetProjectionROIsBLPixelPositionOnDetector() const { return m_roiBLPixel; }
+    void SetProjectionROIsBLPixelPositionOnDetector(Size2D p) { m_roiBLPixel = p; }
     PixelSpacing projectionsPixelSpacing() const { return m_pixel; }
     PixelSpacing projectionsRoisPixelSpacing() const { return m_pixel; }
     Size3D volumeSize3D() const { return m_size; }
@@ -499,6 +509,7 @@ private:
     float m_srcX = 0.f, m_srcZ = 0.f;
     std::vector<Position2D> m_roiBL;
     Size2D m_roiSize;
+    Size2D m_roiBLPixel;
     PixelSpacing m_pixel;
     WSize3D m_fulcrum;
     float m_detZ = 0.f;
