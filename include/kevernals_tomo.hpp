@@ -553,11 +553,63 @@ inline std::shared_ptr<PlanHandle> make_plan(const TomoGeometry *g, kv_family fa
     return h;
 }
 
-inline void write_raw(const std::string &path, const ImageDataPtr &img) {
-    std::ofstream f(path, std::ios::binary);
-    f.write(reinterpret_cast<const char *>(img->data()), (std::streamsize)(img->size() * sizeof(float)));
-}
 }  // namespace kvtomo_detail
+
+namespace kvtomo_detail {
+
+// Baseline TIFF, little endian, uncompressed, one strip per page, one page
+// per z slice; samples of `bytes` bytes, SampleFormat 1 (unsigned) or 3 (IEEE).
+inline bool write_tiff_pages(const std::string &path, int w, int h, int pages, int bytes, int sample_format,
+                             const uint8_t *data) {
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return false;
+    auto put16 = [&](uint16_t v) { f.put((char)(v & 0xFF)); f.put((char)(v >> 8)); };
+    auto put32 = [&](uint32_t v) { for (int i = 0; i < 4; ++i) f.put((char)((v >> (8 * i)) & 0xFF)); };
+    const uint32_t page_bytes = (uint32_t)w * h * bytes;
+    const int ntags = 11;
+    const uint32_t ifd_bytes = 2 + ntags * 12 + 4;
+    f.write("II", 2);
+    put16(42);
+    put32(8);                                    // first IFD right after the header
+    uint32_t off = 8;
+    for (int p = 0; p < pages; ++p) {
+        const uint32_t data_off = off + ifd_bytes;
+        const uint32_t next = p + 1 < pages ? data_off + page_bytes : 0;
+        put16(ntags);
+        auto tag = [&](uint16_t t, uint16_t type, uint32_t count, uint32_t value) {
+            put16(t); put16(type); put32(count);
+            if (type == 3 && count == 1) { put16((uint16_t)value); put16(0); }
+            else put32(value);
+        };
+        tag(256, 4, 1, (uint32_t)w);             // ImageWidth
+        tag(257, 4, 1, (uint32_t)h);             // ImageLength
+        tag(258, 3, 1, (uint32_t)(8 * bytes));   // BitsPerSample
+        tag(259, 3, 1, 1);                       // Compression: none
+        tag(262, 3, 1, 1);                       // Photometric: black is zero
+        tag(273, 4, 1, data_off);                // StripOffsets
+        tag(277, 3, 1, 1);                       // SamplesPerPixel
+        tag(278, 4, 1, (uint32_t)h);             // RowsPerStrip
+        tag(279, 4, 1, page_bytes);              // StripByteCounts
+        tag(284, 3, 1, 1);                       // PlanarConfiguration: contiguous
+        tag(339, 3, 1, (uint32_t)sample_format); // SampleFormat
+        put32(next);
+        // rows top first: memory row h-1 is the image's top row
+        const uint8_t *page = data + (size_t)p * page_bytes;
+        for (int y = h - 1; y >= 0; --y) f.write(reinterpret_cast<const char *>(page + (size_t)y * w * bytes), (std::streamsize)w * bytes);
+        off = data_off + page_bytes;
+    }
+    return (bool)f;
+}
+
+}  // namespace kvtomo_detail
+
+// Float32 volume (or projection stack) to a multi-page TIFF.
+inline bool WriteTIFF(const std::string &path, const ImageDataPtr &img) {
+    const int *d = img->GetDimensions();
+    return kvtomo_detail::write_tiff_pages(path, d[0], d[1], d[2], 4, 3,
+                                           reinterpret_cast<const uint8_t *>(img->data()));
+}
+
 
 class Projector {
 public:
@@ -650,12 +702,14 @@ inline Result<ImageDataPtr> iterate(bool mlem, TomoGeometry *g, ImageDataPtr pro
         if (run(plan, proj->data(), x->data(), iters, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
         return x;
     }
-    // verbose mode: one file per iteration, as the reference writes TIFFs
-    // (Reconstructors.h:47-53, 125-131); raw float32 here.
-    kvtomo_detail::write_raw(outDir.value() + "initialVolume.raw", x);
+    // verbose mode: the initial volume and every iterate as multi-page TIFFs,
+    // named as the reference names them (Reconstructors.h:47-53, 125-131); the
+    // per-iteration projection dumps are not written (the fused kernels keep
+    // them on the device)
+    WriteTIFF(outDir.value() + "initialVolume.tiff", x);
     for (int it = 0; it < iters; ++it) {
         if (run(plan, proj->data(), x->data(), 1, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
-        kvtomo_detail::write_raw(outDir.value() + "reconstructionstep" + std::to_string(it) + ".raw", x);
+        WriteTIFF(outDir.value() + "reconstructionstep" + std::to_string(it) + ".tiff", x);
     }
     return x;
 }
