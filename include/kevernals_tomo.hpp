@@ -744,6 +744,29 @@ inline Result<ImageDataPtr> BackProjection(TomoGeometry *p_tomoGeometry, ImageDa
     return out;
 }
 
+// Filtered backprojection (kv_fbp): Shepp-Logan ramp along the sweep
+// direction, exact transpose, sensitivity normalisation.  No reference
+// counterpart (the reference's "FBP" reconstructor backprojects unfiltered
+// data); always the EXACT family.
+inline Result<ImageDataPtr> FilteredBackProjection(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
+                                                   int p_halfTaps = 128) {
+    if (p_tomoGeometry == nullptr || p_projectionImages == nullptr)
+        return ReconstructorsErrorCode::BackProjectionFailed;
+    Projector projector{p_tomoGeometry, KV_FAMILY_EXACT};
+    kv_plan *plan = projector.plan();
+    if (plan == nullptr || p_projectionImages->size() != kv_plan_proj_elems(plan))
+        return ReconstructorsErrorCode::BackProjectionFailed;
+    auto out = ImageData::New();
+    const auto sz = p_tomoGeometry->volumeSize3D();
+    const auto sp = p_tomoGeometry->volumeVoxelSpacing();
+    out->SetDimensions(sz.x, sz.y, sz.z);
+    out->SetSpacing(sp.x, sp.y, sp.z);
+    out->AllocateScalars();
+    if (kv_fbp(plan, p_projectionImages->data(), out->data(), p_halfTaps, KV_MEM_HOST) != KV_OK)
+        return ReconstructorsErrorCode::BackProjectionFailed;
+    return out;
+}
+
 // recons::ShiftAndAdd, Reconstructors.h:263-379: one detector-sized slice per
 // volume slice.
 inline Result<ImageDataPtr> ShiftAndAdd(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,

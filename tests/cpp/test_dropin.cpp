@@ -83,6 +83,14 @@ int main(int argc, char **argv) {
     projector.PerformProjection(volume, sources[0], single);
     dump(out + "rc_single.raw", single);
 
+    auto fbp = recons::FilteredBackProjection(&geom, efwd, 16);
+    if (!fbp) return 12;
+    dump(out + "exact_fbp.raw", fbp.value());
+    // verbose mode: TIFF dumps of the initial volume and every iterate
+    auto xv = image(nx, ny, nz, std::vector<float>(vol.size(), 1.f).data());
+    auto verbose = recons::MLEM(&geom, projections, 2, 0.5f, xv, out + "verbose_");
+    if (!verbose) return 13;
+
     // error convention: a null initial volume is reported, not fatal
     auto bad = recons::MLEM(&geom, projections, 1, 1.f, ImageDataPtr{}, std::nullopt);
     if (bad || bad.error() != ReconstructorsErrorCode::ART) return 10;

@@ -57,3 +57,14 @@ def test_cpp_dropin(tmp_path):
     eo = O.exact_forward(g, vol.astype(np.float64))
     assert np.linalg.norm(e - eo) <= 2e-6 * np.linalg.norm(eo)
     assert np.array_equal(load("rc_single.raw", (g.nv, g.nu)), proj[0])
+    fbp = load("exact_fbp.raw", g.volume_shape).astype(np.float64)
+    ref = O.exact_fbp(g, load("exact_fwd.raw", g.proj_shape), 16)
+    assert np.linalg.norm(fbp - ref) <= 1e-5 * np.linalg.norm(ref)
+    # verbose MLEM: TIFF pages (rows top first) equal the iterates
+    from test_output_tools import read_tiff
+    x = ones
+    for it in range(2):
+        x = O.rc_mlem(g, proj, x, 1, 0.5)
+        got = read_tiff(str(tmp_path / f"verbose_reconstructionstep{it}.tiff"))[:, ::-1, :]
+        assert np.array_equal(got, x)
+    assert np.array_equal(read_tiff(str(tmp_path / "verbose_initialVolume.tiff"))[:, ::-1, :], ones)
