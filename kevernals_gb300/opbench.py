@@ -9,7 +9,7 @@ rc_back, saa, phantom, unet_fwd, unet_train.  Workloads: chest (1024x1024x128,
 Inputs are device-resident; each line gives the median time of `reps` calls
 (CUDA events around each call), the algorithmic bytes of one call (every
 input read once, every output written once) and the rate they imply.  Also
-the driver for the per-kernel ncu captures (run it with --reps 1 --warmup 0
+the program run under ncu for the per-kernel captures (run it with --reps 1 --warmup 0
 under ncu's kernel filter).
 """
 from __future__ import annotations

@@ -7,7 +7,7 @@ exactly one SART step from zero (kv_sart, relax 1).  Target: the MLEM iterate
 after `target_iters` iterations from the uniform start.  Training triples
 (phantom, shift-and-add, MLEM target) are generated by the engine itself.
 
-warm_start_mlem() keeps plain MLEM as the judge: the network's estimate is
+warm_start_mlem() keeps plain MLEM as the arbiter: the network's estimate is
 used only if its data residual ||A x0 - p|| / ||p|| is no worse than the
 uniform start's; otherwise MLEM starts from the uniform volume.
 

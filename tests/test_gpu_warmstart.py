@@ -6,7 +6,7 @@ U-Net is trained briefly, and on held-out phantoms the number of MLEM
 iterations needed to reach the residual of 15 plain MLEM iterations (within
 1%) is compared for three starts: uniform (plain MLEM), the shift-and-add
 volume alone (the untrained network is the identity), and the trained
-network.  Plain MLEM stays the judge: a start with a worse residual than the
+network.  Plain MLEM stays the arbiter: a start with a worse residual than the
 uniform start is rejected.
 """
 import numpy as np
