@@ -173,7 +173,12 @@ kv_status kv_phantom_ellipsoids(kv_ctx *ctx, int32_t nx, int32_t ny, int32_t nz,
 /* ---- iterative drivers -------------------------------------------------- */
 /* MLEM.  RC: q = A x; where q != 0, q <- relax * p / q; x <- x * B(q), the
  * reference semantics.  EXACT: x <- x * A^T(relax * p / A x) / A^T 1.  The
- * volume is updated in place, as the reference does with its initial volume. */
+ * volume is updated in place, as the reference does with its initial volume.
+ * With KV_MEM_HOST buffers (EXACT, FP32, no callback) the uploads and the
+ * final download overlap the first forward projection and the last
+ * backprojection on an internal copy stream; the call still returns only
+ * when the volume is back in host memory, and the result equals the
+ * KV_MEM_DEVICE call bit for bit. */
 kv_status kv_mlem(kv_plan *plan, const float *projections, float *volume_inout, int iterations,
                   float relax, kv_mem mem, kv_iter_cb cb, void *user);
 /* Simultaneous ART.  RC: x <- x + B(relax * (p - A x)) (recons::ART).  EXACT:

@@ -3,6 +3,7 @@
 // kv_rc.cu and kv_misc.cu.
 #include "kv_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -193,6 +194,9 @@ void ctx_free(kv_ctx *ctx) {
         cudaEventDestroy(r.stop);
     }
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (cudaEvent_t e : ctx->copy_events) cudaEventDestroy(e);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     cudaFree(ctx->d_red);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -652,11 +656,98 @@ kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax,
     return KV_OK;
 }
 
+// Host-buffer MLEM / SART of the EXACT family in FP32 without a callback.
+// The volume and then the projections, kOverlapChunks view chunks, go up on
+// the context's copy stream; the first forward projection runs chunk by
+// chunk, each chunk as soon as its projections have landed.  The last
+// backprojection runs in kOverlapChunks slabs of slices and each slab is
+// copied back while the next ones are computed.  Per ray and per voxel the
+// arithmetic is that of the whole-volume launches, so the result equals the
+// device-buffer call bit for bit.
+constexpr int kOverlapChunks = 8;
+
+kv_status ensure_copy_stream(kv_ctx *ctx) {
+    if (ctx->copy_stream == nullptr)
+        KV_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while (ctx->copy_events.size() < 1 + 2 * kOverlapChunks) {
+        cudaEvent_t e;
+        KV_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->copy_events.push_back(e);
+    }
+    return KV_OK;
+}
+
+kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int iters, float relax, bool mlem) {
+    kv_ctx *ctx = plan->ctx;
+    const kv_geometry &g = plan->g;
+    const size_t D = (size_t)g.nu * g.nv, plane = (size_t)g.nx * g.ny;
+    float *pd = plan->d_proj32, *xd = plan->d_vol32;
+    cudaStream_t cs = ctx->copy_stream, st = ctx->stream;
+    cudaEvent_t *ev = ctx->copy_events.data();
+    const FwdMode fm = mlem ? FWD_MLEM : FWD_SART;
+    const BackMode bm = mlem ? BACK_MLEM : BACK_SART;
+    const FwdArgs fa{xd, pd, plan->d_ratio, nullptr, relax};
+    const BackArgs ba{plan->d_ratio, xd, plan->d_sens, relax};
+    // earlier work on the context stream may still read the staging buffers
+    KV_CHECK_CUDA(ctx, cudaEventRecord(ev[0], st));
+    KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, ev[0], 0));
+    KV_CHECK_CUDA(ctx, cudaMemcpyAsync(xd, volume, plan->nvox * sizeof(float), cudaMemcpyHostToDevice, cs));
+    const int vc = (g.n_views + kOverlapChunks - 1) / kOverlapChunks;
+    for (int c = 0, v0 = 0; v0 < g.n_views; v0 += vc, ++c) {
+        const int n = std::min(vc, g.n_views - v0);
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(pd + v0 * D, proj + v0 * D, n * D * sizeof(float),
+                                           cudaMemcpyHostToDevice, cs));
+        KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + c], cs));
+        KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ev[1 + c], 0));
+        KV_TRY(exact_forward_views_launch(plan, v0, n, fm, fa));
+    }
+    if (iters > 1) {
+        KV_TRY(exact_back_launch(plan, bm, ba));
+        if (iters > 2) KV_TRY(iterate(plan, pd, xd, iters - 2, relax, mlem, nullptr, nullptr));
+        KV_TRY(exact_forward_launch(plan, plan->ex, g.n_views, fm, fa));
+    }
+    const int zc = (g.nz + kOverlapChunks - 1) / kOverlapChunks;
+    for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
+        KV_TRY(exact_back_slab_launch(plan, bm, ba, z0, std::min(zc, g.nz - z0)));
+        KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + kOverlapChunks + c], st));
+    }
+    for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
+        const int n = std::min(zc, g.nz - z0);
+        KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, ev[1 + kOverlapChunks + c], 0));
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(volume + z0 * plane, xd + z0 * plane, n * plane * sizeof(float),
+                                           cudaMemcpyDeviceToHost, cs));
+    }
+    return KV_OK;
+}
+
+kv_status driver_overlapped(kv_plan *plan, const float *proj, float *volume, int iters, float relax, bool mlem) {
+    kv_ctx *ctx = plan->ctx;
+    KV_TRY(ensure(ctx, &plan->d_proj32, plan->nproj * sizeof(float)));
+    KV_TRY(ensure(ctx, &plan->d_vol32, plan->nvox * sizeof(float)));
+    KV_TRY(ensure(ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
+    KV_TRY(ensure_sens(plan));
+    KV_TRY(ensure_copy_stream(ctx));
+    kv_status s = overlapped_body(plan, proj, volume, iters, relax, mlem);
+    // the caller's buffers are released only when no copy is in flight
+    cudaError_t e1 = cudaStreamSynchronize(ctx->copy_stream);
+    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (s != KV_OK) return s;
+    if (e1 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e1));
+    if (e2 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "stream: %s", cudaGetErrorString(e2));
+    return KV_OK;
+}
+
 kv_status driver(kv_plan *plan, const float *proj, float *volume, int iters, float relax, kv_mem mem,
                  kv_iter_cb cb, void *user, bool mlem) {
     KV_TRY(check_common(plan, proj, volume, mem));
     if (iters < 0) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "negative iteration count");
     if (!std::isfinite(relax)) return kv_fail(plan->ctx, KV_ERR_NUMERIC, "non-finite relaxation");
+    if (mem == KV_MEM_HOST && plan->family == KV_FAMILY_EXACT && plan->storage == KV_STORAGE_F32 &&
+        cb == nullptr && iters >= 1) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(plan->ctx->stream, &cs);
+        if (cs == cudaStreamCaptureStatusNone) return driver_overlapped(plan, proj, volume, iters, relax, mlem);
+    }
     float *pd, *xd;
     KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
     KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &xd));

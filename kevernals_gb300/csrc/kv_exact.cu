@@ -442,8 +442,9 @@ __device__ __forceinline__ void back_tile(const ExGeom &G, const ExactTables &T,
 
 template <typename VolT, typename ProjT, int ACC, int MODE>
 __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T, BackArgs a,
-                                                         double *sens_out) {
-    back_tile<VolT, ProjT, ACC, MODE>(G, T, a, sens_out, blockIdx.x, blockIdx.y, blockIdx.z);
+                                                         double *sens_out, int z0) {
+    // slices z0 .. z0 + gridDim.z - 1 (z0 = 0 and gridDim.z = nz for the whole volume)
+    back_tile<VolT, ProjT, ACC, MODE>(G, T, a, sens_out, blockIdx.x, blockIdx.y, z0 + (int)blockIdx.z);
 }
 
 ExGeom exgeom(const kv_plan *plan, int n_views) {
@@ -562,24 +563,24 @@ kv_status fwd_dispatch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
 }
 
 template <typename VolT, typename ProjT>
-kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan) {
+kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan, int z0, int nzs) {
     ExGeom G = exgeom(plan, plan->g.n_views);
     dim3 block(32, plan->back_by);
-    dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
+    dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, nzs);
     cudaStream_t st = plan->ctx->stream;
     const ExactTables &t = plan->ex;
     LaunchTimer lt(plan->ctx, "exact_back");
     if (kahan) {
         switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
         }
     } else {
         switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr); break;
+        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
         }
     }
     KV_CHECK_LAUNCH(plan->ctx, "exact_back_kernel");
@@ -614,13 +615,41 @@ kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int P, FwdMo
     return s;
 }
 
-kv_status exact_back_launch(kv_plan *plan, BackMode mode, const BackArgs &a) {
+// Forward projection of views [v0, v0 + n) only: the per-view tables and the
+// projection buffers are offset to view v0, so every ray computes what the
+// whole-plan launch computes for it.  No reduction (a.red must be null).
+kv_status exact_forward_views_launch(kv_plan *plan, int v0, int n, FwdMode mode, const FwdArgs &a) {
+    const kv_geometry &g = plan->g;
+    if (v0 < 0 || n < 1 || v0 + n > g.n_views || a.red != nullptr)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad view range for the forward projection");
+    ExactTables t = plan->ex;
+    t.xt += (size_t)v0 * g.nu;
+    t.xi += (size_t)v0 * g.nu;
+    t.yt += (size_t)v0 * g.nv;
+    t.yi += (size_t)v0 * g.nv;
+    t.vinfo += v0;
+    t.hr += (size_t)v0 * (g.nz + 1);
+    t.rng += (size_t)v0 * (g.nz + 1);
+    const size_t off = (size_t)v0 * g.nu * g.nv * kv_storage_bytes(plan->storage);
+    FwdArgs b = a;
+    if (b.meas != nullptr) b.meas = static_cast<const char *>(b.meas) + off;
+    b.out = static_cast<char *>(b.out) + off;
+    return exact_forward_launch(plan, t, n, mode, b);
+}
+
+kv_status exact_back_slab_launch(kv_plan *plan, BackMode mode, const BackArgs &a, int z0, int nzs) {
     if (plan->back_by < 1 || plan->back_by > 8) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad back block");
+    if (z0 < 0 || nzs < 1 || z0 + nzs > plan->g.nz)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad slice range for the backprojection");
     switch (plan->storage) {
-    case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, true);
-    case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, true);
-    default: return back_dispatch<float, float>(plan, mode, a, false);
+    case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, true, z0, nzs);
+    case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, true, z0, nzs);
+    default: return back_dispatch<float, float>(plan, mode, a, false, z0, nzs);
     }
+}
+
+kv_status exact_back_launch(kv_plan *plan, BackMode mode, const BackArgs &a) {
+    return exact_back_slab_launch(plan, mode, a, 0, plan->g.nz);
 }
 
 kv_status exact_prescale_launch(kv_plan *plan, const float *y, void *yp) {
@@ -654,7 +683,7 @@ kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
     {
         LaunchTimer lt(plan->ctx, "exact_back_sens_f64");
-        exact_back_kernel<float, float, ACC_DF, BACK_PLAIN><<<grid, block, 0, st>>>(G, plan->ex, a, sens);
+        exact_back_kernel<float, float, ACC_DF, BACK_PLAIN><<<grid, block, 0, st>>>(G, plan->ex, a, sens, 0);
     }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(ls, st);
@@ -912,7 +941,7 @@ float time_back(kv_ctx *ctx, const ExGeom &G, const ExactTables &T, const void *
     float best = 1e30f;
     for (int rep = 0; rep < 2; ++rep) {
         cudaEventRecord(e0, ctx->stream);
-        exact_back_kernel<VolT, ProjT, ACC, BACK_PLAIN><<<grid, block, 0, ctx->stream>>>(G, T, a, nullptr);
+        exact_back_kernel<VolT, ProjT, ACC, BACK_PLAIN><<<grid, block, 0, ctx->stream>>>(G, T, a, nullptr, 0);
         cudaEventRecord(e1, ctx->stream);
         cudaEventSynchronize(e1);
         float ms = 0.f;

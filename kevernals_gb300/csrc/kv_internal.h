@@ -36,6 +36,10 @@ struct kv_ctx {
     bool timing = false;
     std::vector<kv_timing_rec> timing_recs;
     std::vector<cudaEvent_t> event_pool;
+    // host-buffer MLEM / SART: copies overlapped with the first forward and
+    // the last backprojection (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> copy_events;
 };
 
 // Brackets one kernel launch with CUDA events on the context stream when the
@@ -210,6 +214,11 @@ void exact_free_tables(ExactTables *t);
 kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int n_views, FwdMode mode,
                                const FwdArgs &a);
 kv_status exact_back_launch(kv_plan *plan, BackMode mode, const BackArgs &a);
+// The same launches restricted to views [v0, v0 + n) (forward, no reduction)
+// and to slices [z0, z0 + nzs) (backprojection); per ray and per voxel the
+// arithmetic is that of the whole launch.
+kv_status exact_forward_views_launch(kv_plan *plan, int v0, int n, FwdMode mode, const FwdArgs &a);
+kv_status exact_back_slab_launch(kv_plan *plan, BackMode mode, const BackArgs &a, int z0, int nzs);
 kv_status exact_sensitivity_launch(kv_plan *plan, double *sens);
 kv_status exact_prescale_launch(kv_plan *plan, const float *y, void *yp);
 
