@@ -174,7 +174,7 @@ kv_status kv_phantom_ellipsoids(kv_ctx *ctx, int32_t nx, int32_t ny, int32_t nz,
 /* MLEM.  RC: q = A x; where q != 0, q <- relax * p / q; x <- x * B(q), the
  * reference semantics.  EXACT: x <- x * A^T(relax * p / A x) / A^T 1.  The
  * volume is updated in place, as the reference does with its initial volume.
- * With KV_MEM_HOST buffers (EXACT, FP32, no callback) the uploads and the
+ * With KV_MEM_HOST buffers (FP32 storage, no callback) the uploads and the
  * final download overlap the first forward projection and the last
  * backprojection on an internal copy stream; the call still returns only
  * when the volume is back in host memory, and the result equals the

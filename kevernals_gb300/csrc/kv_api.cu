@@ -656,7 +656,7 @@ kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax,
     return KV_OK;
 }
 
-// Host-buffer MLEM / SART of the EXACT family in FP32 without a callback.
+// Host-buffer MLEM / SART (both families, FP32 storage) without a callback.
 // The volume and then the projections, kOverlapChunks view chunks, go up on
 // the context's copy stream; the first forward projection runs chunk by
 // chunk, each chunk as soon as its projections have landed.  The last
@@ -677,6 +677,25 @@ kv_status ensure_copy_stream(kv_ctx *ctx) {
     return KV_OK;
 }
 
+// The fused update step of either family on views [v0, v0 + n) (forward +
+// ratio) and on slices [z0, z0 + n) (backprojection + update).
+kv_status update_forward_views(kv_plan *plan, bool mlem, const float *pd, const float *xd, float relax, int v0,
+                               int n) {
+    if (plan->family == KV_FAMILY_EXACT)
+        return exact_forward_views_launch(plan, v0, n, mlem ? FWD_MLEM : FWD_SART,
+                                          FwdArgs{xd, pd, plan->d_ratio, nullptr, relax});
+    const size_t off = (size_t)v0 * plan->g.nu * plan->g.nv;
+    return rc_forward_launch(plan, plan->d_src + 3 * (size_t)v0, plan->d_org + 3 * (size_t)v0, n,
+                             mlem ? RC_MLEM : RC_ART, xd, pd + off, (float *)plan->d_ratio + off, relax);
+}
+
+kv_status update_back_slab(kv_plan *plan, bool mlem, float *xd, float relax, int z0, int n) {
+    if (plan->family == KV_FAMILY_EXACT)
+        return exact_back_slab_launch(plan, mlem ? BACK_MLEM : BACK_SART,
+                                      BackArgs{plan->d_ratio, xd, plan->d_sens, relax}, z0, n);
+    return rc_back_slab_launch(plan, mlem ? RC_MLEM : RC_ART, (const float *)plan->d_ratio, xd, z0, n);
+}
+
 kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int iters, float relax, bool mlem) {
     kv_ctx *ctx = plan->ctx;
     const kv_geometry &g = plan->g;
@@ -684,10 +703,6 @@ kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int i
     float *pd = plan->d_proj32, *xd = plan->d_vol32;
     cudaStream_t cs = ctx->copy_stream, st = ctx->stream;
     cudaEvent_t *ev = ctx->copy_events.data();
-    const FwdMode fm = mlem ? FWD_MLEM : FWD_SART;
-    const BackMode bm = mlem ? BACK_MLEM : BACK_SART;
-    const FwdArgs fa{xd, pd, plan->d_ratio, nullptr, relax};
-    const BackArgs ba{plan->d_ratio, xd, plan->d_sens, relax};
     // earlier work on the context stream may still read the staging buffers
     KV_CHECK_CUDA(ctx, cudaEventRecord(ev[0], st));
     KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, ev[0], 0));
@@ -699,16 +714,16 @@ kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int i
                                            cudaMemcpyHostToDevice, cs));
         KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + c], cs));
         KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ev[1 + c], 0));
-        KV_TRY(exact_forward_views_launch(plan, v0, n, fm, fa));
+        KV_TRY(update_forward_views(plan, mlem, pd, xd, relax, v0, n));
     }
     if (iters > 1) {
-        KV_TRY(exact_back_launch(plan, bm, ba));
+        KV_TRY(update_back_slab(plan, mlem, xd, relax, 0, g.nz));
         if (iters > 2) KV_TRY(iterate(plan, pd, xd, iters - 2, relax, mlem, nullptr, nullptr));
-        KV_TRY(exact_forward_launch(plan, plan->ex, g.n_views, fm, fa));
+        KV_TRY(update_forward_views(plan, mlem, pd, xd, relax, 0, g.n_views));
     }
     const int zc = (g.nz + kOverlapChunks - 1) / kOverlapChunks;
     for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
-        KV_TRY(exact_back_slab_launch(plan, bm, ba, z0, std::min(zc, g.nz - z0)));
+        KV_TRY(update_back_slab(plan, mlem, xd, relax, z0, std::min(zc, g.nz - z0)));
         KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + kOverlapChunks + c], st));
     }
     for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
@@ -725,7 +740,7 @@ kv_status driver_overlapped(kv_plan *plan, const float *proj, float *volume, int
     KV_TRY(ensure(ctx, &plan->d_proj32, plan->nproj * sizeof(float)));
     KV_TRY(ensure(ctx, &plan->d_vol32, plan->nvox * sizeof(float)));
     KV_TRY(ensure(ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
-    KV_TRY(ensure_sens(plan));
+    if (plan->family == KV_FAMILY_EXACT) KV_TRY(ensure_sens(plan));
     KV_TRY(ensure_copy_stream(ctx));
     kv_status s = overlapped_body(plan, proj, volume, iters, relax, mlem);
     // the caller's buffers are released only when no copy is in flight
@@ -742,8 +757,7 @@ kv_status driver(kv_plan *plan, const float *proj, float *volume, int iters, flo
     KV_TRY(check_common(plan, proj, volume, mem));
     if (iters < 0) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "negative iteration count");
     if (!std::isfinite(relax)) return kv_fail(plan->ctx, KV_ERR_NUMERIC, "non-finite relaxation");
-    if (mem == KV_MEM_HOST && plan->family == KV_FAMILY_EXACT && plan->storage == KV_STORAGE_F32 &&
-        cb == nullptr && iters >= 1) {
+    if (mem == KV_MEM_HOST && plan->storage == KV_STORAGE_F32 && cb == nullptr && iters >= 1) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(plan->ctx->stream, &cs);
         if (cs == cudaStreamCaptureStatusNone) return driver_overlapped(plan, proj, volume, iters, relax, mlem);

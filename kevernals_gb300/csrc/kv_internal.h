@@ -226,6 +226,8 @@ kv_status rc_forward_launch(kv_plan *plan, const float *d_src, const float *d_or
                             int mode, const float *vol, const float *meas, float *out,
                             float relax);
 kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol);
+// slices [z0, z0 + nzs) only; per voxel the arithmetic of the whole launch
+kv_status rc_back_slab_launch(kv_plan *plan, int mode, const float *proj, float *vol, int z0, int nzs);
 
 kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out);
 kv_status ramp_filter_launch(kv_plan *plan, const float *in, float *out, int half_taps);

@@ -173,10 +173,10 @@ template <int MODE>
 __global__ void __launch_bounds__(128) rc_back_kernel(RcGeom G, const float *__restrict__ src,
                                                       const float *__restrict__ org,
                                                       const float *__restrict__ proj,
-                                                      float *__restrict__ vol) {
+                                                      float *__restrict__ vol, int z0) {
     const int x = blockIdx.x * 32 + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
+    const int z = z0 + (int)blockIdx.z;   // slices z0 .. z0 + gridDim.z - 1
     if (x >= G.nx || y >= G.ny) return;
     const float tol = 0.000000000000000000000001F;
     const int semi = 5;
@@ -281,18 +281,24 @@ kv_status rc_forward_launch(kv_plan *plan, const float *d_src, const float *d_or
     return KV_OK;
 }
 
-kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol) {
+kv_status rc_back_slab_launch(kv_plan *plan, int mode, const float *proj, float *vol, int z0, int nzs) {
+    if (z0 < 0 || nzs < 1 || z0 + nzs > plan->g.nz)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad slice range for the backprojection");
     RcGeom G = rcgeom(plan, plan->g.n_views);
-    dim3 block(32, 4), grid((G.nx + 31) / 32, (G.ny + 3) / 4, G.nz);
+    dim3 block(32, 4), grid((G.nx + 31) / 32, (G.ny + 3) / 4, nzs);
     cudaStream_t st = plan->ctx->stream;
     LaunchTimer lt(plan->ctx, "rc_back");
     switch (mode) {
-    case RC_PLAIN: rc_back_kernel<RC_PLAIN><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol); break;
-    case RC_MLEM: rc_back_kernel<RC_MLEM><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol); break;
-    default: rc_back_kernel<RC_ART><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol); break;
+    case RC_PLAIN: rc_back_kernel<RC_PLAIN><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol, z0); break;
+    case RC_MLEM: rc_back_kernel<RC_MLEM><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol, z0); break;
+    default: rc_back_kernel<RC_ART><<<grid, block, 0, st>>>(G, plan->d_src, plan->d_org, proj, vol, z0); break;
     }
     KV_CHECK_LAUNCH(plan->ctx, "rc_back_kernel");
     return KV_OK;
+}
+
+kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol) {
+    return rc_back_slab_launch(plan, mode, proj, vol, 0, plan->g.nz);
 }
 
 kv_status residual_reduce_launch(kv_ctx *ctx, const float *q, const float *p, size_t n, double *red);

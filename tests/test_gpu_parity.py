@@ -251,16 +251,17 @@ def test_device_buffers_match_host(ctx):
         assert np.array_equal(bd.cpu().numpy(), bh)
 
 
+@pytest.mark.parametrize("family", ["exact", "rc"])
 @pytest.mark.parametrize("gi", [0, 1, 2])
-def test_host_mlem_sart_overlapped_equal_device(ctx, gi):
-    """Host-buffer MLEM / SART (EXACT, FP32) overlap the copies with the first
+def test_host_mlem_sart_overlapped_equal_device(ctx, gi, family):
+    """Host-buffer MLEM / SART (FP32) overlap the copies with the first
     forward projection (view chunks) and the last backprojection (slabs of
     slices); the result equals the device-buffer call bit for bit for 1 to 4
     iterations, with ragged chunks (5, 4 and 9 views; 12, 7 and 16 slices)."""
     torch = pytest.importorskip("torch")
     g = small_geoms()[gi]
     p = O.exact_forward(g, phantom_for(g).astype(np.float64)).astype(np.float32)
-    plan = engine.Plan(ctx, g, "exact")
+    plan = engine.Plan(ctx, g, family)
     pd = torch.from_numpy(p).cuda()
     for iters in (1, 2, 3, 4):
         for method, relax, x0 in (("mlem", 1.0, 1.0), ("sart", 0.5, 0.0)):
