@@ -134,6 +134,60 @@ kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_
     return KV_OK;
 }
 
+// Host-buffer calls overlap their copies with the kernels on a second
+// (non-blocking) stream of the context, in kOverlapChunks pieces.
+constexpr int kOverlapChunks = 8;
+
+kv_status ensure_copy_stream(kv_ctx *ctx) {
+    if (ctx->copy_stream == nullptr)
+        KV_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    while (ctx->copy_events.size() < 1 + 2 * kOverlapChunks) {
+        cudaEvent_t e;
+        KV_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->copy_events.push_back(e);
+    }
+    return KV_OK;
+}
+
+// Runs launch(i0, n) on the context stream for kOverlapChunks pieces of
+// [0, total) and copies each piece's output (dev + i0 * stride, n * stride
+// floats) to the same place in host memory on the copy stream as soon as
+// that piece's kernels are done.  Events ev0 .. ev0 + kOverlapChunks - 1.
+template <typename Launch>
+kv_status pieces_to_host_body(kv_ctx *ctx, int total, size_t stride, const float *dev, float *host, int ev0,
+                              Launch &launch) {
+    cudaEvent_t *ev = ctx->copy_events.data() + ev0;
+    const int pc = (total + kOverlapChunks - 1) / kOverlapChunks;
+    for (int c = 0, i0 = 0; i0 < total; i0 += pc, ++c) {
+        KV_TRY(launch(i0, std::min(pc, total - i0)));
+        KV_CHECK_CUDA(ctx, cudaEventRecord(ev[c], ctx->stream));
+    }
+    for (int c = 0, i0 = 0; i0 < total; i0 += pc, ++c) {
+        const size_t n = (size_t)std::min(pc, total - i0) * stride;
+        KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev[c], 0));
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(host + i0 * stride, dev + i0 * stride, n * sizeof(float),
+                                           cudaMemcpyDeviceToHost, ctx->copy_stream));
+    }
+    return KV_OK;
+}
+
+// Waits for both streams, so that no copy is in flight when the caller's
+// buffers are handed back; returns the first error.
+kv_status sync_both(kv_ctx *ctx, kv_status s) {
+    cudaError_t e1 = cudaStreamSynchronize(ctx->copy_stream);
+    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (s != KV_OK) return s;
+    if (e1 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e1));
+    if (e2 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "stream: %s", cudaGetErrorString(e2));
+    return KV_OK;
+}
+
+bool stream_capturing(kv_ctx *ctx) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &cs);
+    return cs != cudaStreamCaptureStatusNone;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -390,6 +444,19 @@ extern "C" kv_status kv_forward(kv_plan *plan, const float *volume, float *proj,
     float *vd, *pd;
     KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &vd));
     KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, false, &pd));
+    if (mem == KV_MEM_HOST && plan->storage == KV_STORAGE_F32 && !stream_capturing(plan->ctx)) {
+        // view chunks, each copied back while the next ones are projected
+        KV_TRY(ensure_copy_stream(plan->ctx));
+        auto fwd = [&](int v0, int n) -> kv_status {
+            if (plan->family == KV_FAMILY_EXACT)
+                return exact_forward_views_launch(plan, v0, n, FWD_PLAIN, FwdArgs{vd, nullptr, pd, nullptr, 1.f});
+            const size_t off = (size_t)v0 * plan->g.nu * plan->g.nv;
+            return rc_forward_launch(plan, plan->d_src + 3 * (size_t)v0, plan->d_org + 3 * (size_t)v0, n,
+                                     RC_PLAIN, vd, nullptr, pd + off, 1.f);
+        };
+        return sync_both(plan->ctx, pieces_to_host_body(plan->ctx, plan->g.n_views,
+                                                        (size_t)plan->g.nu * plan->g.nv, pd, proj, 1, fwd));
+    }
     if (plan->family == KV_FAMILY_RC) {
         KV_TRY(rc_forward_launch(plan, plan->d_src, plan->d_org, plan->g.n_views, RC_PLAIN, vd, nullptr, pd, 1.f));
     } else if (plan->storage == KV_STORAGE_F32) {
@@ -439,6 +506,21 @@ extern "C" kv_status kv_back(kv_plan *plan, const float *proj, float *volume, kv
     float *pd, *vd;
     KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
     KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, false, &vd));
+    if (mem == KV_MEM_HOST && plan->storage == KV_STORAGE_F32 && !stream_capturing(plan->ctx)) {
+        // slabs of slices, each copied back while the next ones are computed
+        KV_TRY(ensure_copy_stream(plan->ctx));
+        if (plan->family == KV_FAMILY_EXACT) {
+            KV_TRY(ensure(plan->ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
+            KV_TRY(exact_prescale_launch(plan, pd, plan->d_ratio));
+        }
+        auto back = [&](int z0, int n) -> kv_status {
+            if (plan->family == KV_FAMILY_EXACT)
+                return exact_back_slab_launch(plan, BACK_PLAIN, BackArgs{plan->d_ratio, vd, nullptr, 1.f}, z0, n);
+            return rc_back_slab_launch(plan, RC_PLAIN, pd, vd, z0, n);
+        };
+        return sync_both(plan->ctx, pieces_to_host_body(plan->ctx, plan->g.nz, (size_t)plan->g.nx * plan->g.ny,
+                                                        vd, volume, 1, back));
+    }
     if (plan->family == KV_FAMILY_RC) {
         KV_TRY(rc_back_launch(plan, RC_PLAIN, pd, vd));
     } else {
@@ -664,18 +746,6 @@ kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax,
 // copied back while the next ones are computed.  Per ray and per voxel the
 // arithmetic is that of the whole-volume launches, so the result equals the
 // device-buffer call bit for bit.
-constexpr int kOverlapChunks = 8;
-
-kv_status ensure_copy_stream(kv_ctx *ctx) {
-    if (ctx->copy_stream == nullptr)
-        KV_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-    while (ctx->copy_events.size() < 1 + 2 * kOverlapChunks) {
-        cudaEvent_t e;
-        KV_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        ctx->copy_events.push_back(e);
-    }
-    return KV_OK;
-}
 
 // The fused update step of either family on views [v0, v0 + n) (forward +
 // ratio) and on slices [z0, z0 + n) (backprojection + update).
@@ -721,18 +791,8 @@ kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int i
         if (iters > 2) KV_TRY(iterate(plan, pd, xd, iters - 2, relax, mlem, nullptr, nullptr));
         KV_TRY(update_forward_views(plan, mlem, pd, xd, relax, 0, g.n_views));
     }
-    const int zc = (g.nz + kOverlapChunks - 1) / kOverlapChunks;
-    for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
-        KV_TRY(update_back_slab(plan, mlem, xd, relax, z0, std::min(zc, g.nz - z0)));
-        KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + kOverlapChunks + c], st));
-    }
-    for (int c = 0, z0 = 0; z0 < g.nz; z0 += zc, ++c) {
-        const int n = std::min(zc, g.nz - z0);
-        KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, ev[1 + kOverlapChunks + c], 0));
-        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(volume + z0 * plane, xd + z0 * plane, n * plane * sizeof(float),
-                                           cudaMemcpyDeviceToHost, cs));
-    }
-    return KV_OK;
+    auto back = [&](int z0, int n) { return update_back_slab(plan, mlem, xd, relax, z0, n); };
+    return pieces_to_host_body(ctx, g.nz, plane, xd, volume, 1 + kOverlapChunks, back);
 }
 
 kv_status driver_overlapped(kv_plan *plan, const float *proj, float *volume, int iters, float relax, bool mlem) {
@@ -742,14 +802,7 @@ kv_status driver_overlapped(kv_plan *plan, const float *proj, float *volume, int
     KV_TRY(ensure(ctx, &plan->d_ratio, plan->nproj * sizeof(float)));
     if (plan->family == KV_FAMILY_EXACT) KV_TRY(ensure_sens(plan));
     KV_TRY(ensure_copy_stream(ctx));
-    kv_status s = overlapped_body(plan, proj, volume, iters, relax, mlem);
-    // the caller's buffers are released only when no copy is in flight
-    cudaError_t e1 = cudaStreamSynchronize(ctx->copy_stream);
-    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
-    if (s != KV_OK) return s;
-    if (e1 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e1));
-    if (e2 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "stream: %s", cudaGetErrorString(e2));
-    return KV_OK;
+    return sync_both(ctx, overlapped_body(plan, proj, volume, iters, relax, mlem));
 }
 
 kv_status driver(kv_plan *plan, const float *proj, float *volume, int iters, float relax, kv_mem mem,
@@ -757,11 +810,9 @@ kv_status driver(kv_plan *plan, const float *proj, float *volume, int iters, flo
     KV_TRY(check_common(plan, proj, volume, mem));
     if (iters < 0) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "negative iteration count");
     if (!std::isfinite(relax)) return kv_fail(plan->ctx, KV_ERR_NUMERIC, "non-finite relaxation");
-    if (mem == KV_MEM_HOST && plan->storage == KV_STORAGE_F32 && cb == nullptr && iters >= 1) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(plan->ctx->stream, &cs);
-        if (cs == cudaStreamCaptureStatusNone) return driver_overlapped(plan, proj, volume, iters, relax, mlem);
-    }
+    if (mem == KV_MEM_HOST && plan->storage == KV_STORAGE_F32 && cb == nullptr && iters >= 1 &&
+        !stream_capturing(plan->ctx))
+        return driver_overlapped(plan, proj, volume, iters, relax, mlem);
     float *pd, *xd;
     KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
     KV_TRY(stage_in(plan, volume, mem, &plan->d_vol32, plan->nvox, true, &xd));
