@@ -307,6 +307,18 @@ def time_to_residual(ctx, g, cfg, rank, plain_iters=50):
             "speedup": r["speedup"], "checkpoint": os.path.relpath(WEIGHTS, ROOT)}
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: replicas finish when the last one does.  One
+    all-reduce (MAX) over the process group; the identity on one rank."""
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
     import torch
 
@@ -357,11 +369,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
     kernels = ctx.read_timing()
     ctx.set_timing(False)
     clocks = sampler.stop()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, f"cuda:{dev}")
     rays_per_step = 2 * g.n_rays
     value = world * rays_per_step * args.steps / (ms * 1e-3)
     gpu_launches = sum(n for n, _ in kernels.values())
@@ -399,12 +407,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
         a1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ems = a0.elapsed_time(a1)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ems], device=f"cuda:{dev}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = max_over_ranks(a0.elapsed_time(a1), world, f"cuda:{dev}")
         e2e = {"value": world * rays_per_step * args.steps / (ems * 1e-3), "unit": UNIT,
                "h2d_bytes_per_step": 4 * (g.n_rays + g.n_voxels), "d2h_bytes_per_step": 4 * g.n_voxels,
                "ms_per_step": ems / args.steps}
