@@ -70,3 +70,23 @@ def test_shift_rule_rejects_degenerate_geometry(lib):
     g = linear_sweep(8, 8, 4, 0.5, 0.5, 1.0, 1, 8, 8, 0.5, 0.5, 10.0)   # one view
     with pytest.raises(_lib.KvError):
         engine.shift_and_add_shifts(g, "exact")
+
+
+def test_cpp_dropin_compiles_and_links(lib, tmp_path):
+    """The C++ drop-in headers (kevernals_tomo.hpp, kevernals_dicom.hpp,
+    kevernals_output.hpp) compile with warnings as errors and the drop-in
+    driver links against libkvtomo.so (running it needs a GPU)."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(__file__))
+    so = os.path.dirname(build.build())
+    src = tmp_path / "all_headers.cpp"
+    src.write_text('#include "kevernals_tomo.hpp"\n#include "kevernals_dicom.hpp"\n'
+                   '#include "kevernals_output.hpp"\nint main() { return 0; }\n')
+    for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp")):
+        r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I",
+                            os.path.join(root, "include"), f, "-o", str(tmp_path / "a.out"), "-L", so,
+                            "-lkvtomo", "-Wl,-rpath," + so], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]

@@ -148,6 +148,33 @@ def test_saa_shift_rules():
     assert np.array_equal(ex[:, 0], -ex[:, -1])
 
 
+def test_fbp_ramp_known_answers():
+    """The FBP oracle's Shepp-Logan kernel h[n] = -2 / (pi^2 (4 n^2 - 1)):
+    h[0] = 2 / pi^2, h[1] = -2 / (3 pi^2); its frequency response is
+    |sin(w / 2)| / pi (the ramp |nu| times the sinc window, nu = w / 2 pi), up
+    to the truncation error sum_{n > K} 2 |h[n]| < 1 / (pi^2 K); filtering an
+    impulse along v reproduces the kernel; filtering is linear and leaves u
+    and the views independent."""
+    h = O.ramp_taps(4096)
+    assert h[0] == 2.0 / np.pi ** 2 and abs(h[1] + 2.0 / (3.0 * np.pi ** 2)) < 1e-17
+    n = np.arange(1, h.size)
+    for w in (0.0, 0.3, np.pi / 3, 2.0, np.pi):
+        resp = h[0] + 2.0 * np.sum(h[1:] * np.cos(n * w))
+        assert abs(resp - abs(np.sin(w / 2.0)) / np.pi) < 1.0 / (np.pi ** 2 * 4096)
+    K, nv = 8, 40
+    p = np.zeros((2, nv, 3))
+    p[1, 20, 2] = 1.0
+    f = O.ramp_filter_v(p, K)
+    hk = O.ramp_taps(K)
+    expect = np.zeros(nv)
+    expect[20 - K:20 + K + 1] = np.concatenate([hk[:0:-1], hk])
+    assert np.array_equal(f[1, :, 2], expect)
+    assert not f[0].any() and not f[1, :, :2].any()
+    rng = np.random.default_rng(3)
+    a, b = rng.random((2, 2, nv, 3))
+    assert np.allclose(O.ramp_filter_v(2.0 * a - b, K), 2.0 * O.ramp_filter_v(a, K) - O.ramp_filter_v(b, K))
+
+
 def test_splitmix64_known_values():
     # first outputs of splitmix64 seeded with 0 (published reference sequence)
     r = ph.SplitMix64(0)
