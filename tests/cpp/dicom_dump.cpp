@@ -6,11 +6,21 @@
 
 #include "kevernals_dicom.hpp"
 
+// a string as the body of a JSON string literal
+static std::string json_escape(const std::string &v) {
+    std::string out;
+    for (char c : v) {
+        if (c == '"' || c == '\\') out += '\\';
+        out += c;
+    }
+    return out;
+}
+
 int main(int argc, char **argv) {
     if (argc < 3) return 2;
     TomoGeometry geo{std::string(argv[1])};
     if (!geo.IsValid()) {
-        std::printf("{\"ok\": false, \"error\": \"geometry: %s\"}\n", geo.ErrorMessage().c_str());
+        std::printf("{\"ok\": false, \"error\": \"geometry: %s\"}\n", json_escape(geo.ErrorMessage()).c_str());
         return 0;
     }
     std::vector<int> remove;
@@ -18,8 +28,8 @@ int main(int argc, char **argv) {
     DICOMReader reader(&geo);
     auto res = reader.ReadDirectory(argv[2], remove);
     if (!res) {
-        std::printf("{\"ok\": false, \"error\": \"%s\", \"code\": \"%s\"}\n", reader.LastError().c_str(),
-                    res.error().message().c_str());
+        std::printf("{\"ok\": false, \"error\": \"%s\", \"code\": \"%s\"}\n",
+                    json_escape(reader.LastError()).c_str(), json_escape(res.error().message()).c_str());
         return 0;
     }
     const auto img = res.value();

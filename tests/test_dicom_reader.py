@@ -113,3 +113,48 @@ def test_read_directory_errors(dumper, tmp_path):
     write_dicom(str(small / "a.dcm"), np.zeros((20, 20), np.uint16), "1")
     out = json.loads(subprocess.run([dumper, geo, str(small)], check=True, capture_output=True, text=True).stdout)
     assert not out["ok"] and "ROI" in out["error"]
+
+
+@pytest.fixture(scope="module")
+def checked_dumper(tmp_path_factory):
+    """The dump tool built with AddressSanitizer and UBSan (plain when the
+    compiler lacks them)."""
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path_factory.mktemp("dicom_asan") / "dicom_dump")
+    base = ["g++", "-std=c++17", "-O1", "-g", "-I", os.path.join(ROOT, "include"),
+            os.path.join(ROOT, "tests", "cpp", "dicom_dump.cpp"), "-o", exe]
+    san = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined"]
+    if subprocess.run(base + san, capture_output=True).returncode != 0:
+        subprocess.run(base, check=True)
+    return exe
+
+
+def test_malformed_files_are_errors_not_crashes(checked_dumper, tmp_path):
+    """Every prefix of a file's header (and a few cuts inside the pixel data)
+    and seeded byte corruptions of the header, in both VR encodings: the
+    reader returns a result or an error with a printable message, within a
+    time limit, with no sanitizer report."""
+    geo = str(tmp_path / "geo.xml")
+    write_xml(geo, roi="10 20 0 0 29 33")
+    rng = np.random.default_rng(5)
+    variants = []
+    for explicit in (True, False):
+        good = tmp_path / f"good_{explicit}.dcm"
+        write_dicom(str(good), rng.integers(0, 4000, (75, 100)).astype(np.uint16), "101500", explicit=explicit)
+        raw = good.read_bytes()
+        hdr = len(raw) - 75 * 100 * 2
+        variants += [raw[:cut] for cut in list(range(0, hdr + 8, 3)) + [hdr + 101, len(raw) - 1]]
+        for _ in range(60):
+            b = bytearray(raw)
+            for pos in rng.integers(128, hdr, size=rng.integers(1, 4)):
+                b[pos] = rng.integers(0, 256)
+            variants.append(bytes(b))
+    d = tmp_path / "series"
+    d.mkdir()
+    for v in variants:
+        (d / "x.dcm").write_bytes(v)
+        r = subprocess.run([checked_dumper, geo, str(d)], capture_output=True, timeout=20)
+        assert r.returncode == 0 and b"ERROR" not in r.stderr and b"runtime error" not in r.stderr, r.stderr[-1500:]
+        out = json.loads(r.stdout.decode("ascii"))
+        assert out["ok"] or out["error"]
