@@ -67,17 +67,6 @@ struct Image {
     std::vector<float> pixels;
 };
 
-// A value read from a file, fit for an error message: printable ASCII only
-// (anything else becomes '?'), at most 64 characters (the longest UID).
-inline std::string printable(const std::string &v) {
-    std::string out;
-    for (size_t i = 0; i < v.size() && i < 64; ++i) {
-        const unsigned char c = static_cast<unsigned char>(v[i]);
-        out += (c >= 0x20 && c < 0x7F) ? static_cast<char>(c) : '?';
-    }
-    return out;
-}
-
 class Parser {
 public:
     Parser(const std::vector<uint8_t> &b) : b_(b) {}
@@ -98,7 +87,7 @@ public:
             if (ts == "1.2.840.10008.1.2") explicit_vr = false;
             else if (ts == "1.2.840.10008.1.2.1") explicit_vr = true;
             else {
-                err = "unsupported transfer syntax " + printable(ts);
+                err = "unsupported transfer syntax " + kvtomo_detail::printable(ts);
                 return false;
             }
         }

@@ -85,6 +85,17 @@ inline const std::error_category &reconstructors_category() {
     static ReconstructorsCategory c;
     return c;
 }
+
+// A value read from a file, fit for an error message: printable ASCII only
+// (anything else becomes '?'), at most 64 characters.
+inline std::string printable(const std::string &v) {
+    std::string out;
+    for (size_t i = 0; i < v.size() && i < 64; ++i) {
+        const unsigned char c = static_cast<unsigned char>(v[i]);
+        out += (c >= 0x20 && c < 0x7F) ? static_cast<char>(c) : '?';
+    }
+    return out;
+}
 }  // namespace kvtomo_detail
 
 namespace std {
@@ -216,16 +227,34 @@ private:
             else return;
         }
     }
+    // the five predefined entities, in one left-to-right pass (so "&amp;lt;"
+    // gives "&lt;"); anything else is kept as written
     static void decode(std::string &t) {
         static const std::pair<const char *, char> ents[] = {
             {"&lt;", '<'}, {"&gt;", '>'}, {"&quot;", '"'}, {"&apos;", '\''}, {"&amp;", '&'}};
-        for (const auto &e : ents) {
-            size_t k;
-            const size_t n = std::char_traits<char>::length(e.first);
-            while ((k = t.find(e.first)) != std::string::npos) t.replace(k, n, 1, e.second);
+        std::string out;
+        out.reserve(t.size());
+        for (size_t i = 0; i < t.size();) {
+            bool hit = false;
+            if (t[i] == '&') {
+                for (const auto &e : ents) {
+                    const size_t n = std::char_traits<char>::length(e.first);
+                    if (t.compare(i, n, e.first) == 0) {
+                        out += e.second;
+                        i += n;
+                        hit = true;
+                        break;
+                    }
+                }
+            }
+            if (!hit) out += t[i++];
         }
+        t.swap(out);
     }
-    bool element(Node &n, std::string &err) {
+    // nesting deeper than this is refused (the geometry schema uses four levels)
+    static constexpr int kMaxDepth = 64;
+    bool element(Node &n, std::string &err, int depth = 0) {
+        if (depth > kMaxDepth) { err = "elements nested too deeply"; return false; }
         if (!starts("<")) { err = "expected an element"; return false; }
         ++i_;
         const size_t b = i_;
@@ -255,7 +284,7 @@ private:
             }
             if (starts("<")) {
                 n.children.emplace_back();
-                if (!element(n.children.back(), err)) return false;
+                if (!element(n.children.back(), err, depth + 1)) return false;
                 continue;
             }
             const size_t e = s_.find('<', i_);
@@ -330,8 +359,19 @@ private:
         const std::string src = ss.str();
         kvxml::Node root;
         std::string err;
-        if (!kvxml::Parser(src).parse(root, err)) { m_error = "XML: " + err; return false; }
+        if (!kvxml::Parser(src).parse(root, err)) {
+            m_error = "XML: " + kvtomo_detail::printable(err);
+            return false;
+        }
         auto fail = [this](const std::string &m) { m_error = m; return false; };
+        // a count as the reference reads it (double -> float -> int), refused
+        // when it is not a positive number up to kMaxAxis
+        auto count = [](double v, int &out) {
+            const float f = static_cast<float>(v);
+            if (!(f >= 1.f && f <= static_cast<float>(kMaxAxis))) return false;
+            out = static_cast<int>(f);
+            return true;
+        };
         using kvxml::Node;
         double v[3];
         const Node *rot = root.child("Rotation");
@@ -345,8 +385,8 @@ private:
         if (!kvxml::triple(grid->child("resolution"), res)) return fail("Grid/resolution missing or unreadable");
         const float cx = static_cast<float>(c[0]), cy = static_cast<float>(c[1]), cz = static_cast<float>(c[2]);
         m_spacing = {static_cast<float>(sc[2]), static_cast<float>(sc[1]), static_cast<float>(sc[0])};
-        m_size = {static_cast<int>(static_cast<float>(res[2])), static_cast<int>(static_cast<float>(res[1])),
-                  static_cast<int>(static_cast<float>(res[0]))};
+        if (!count(res[2], m_size.x) || !count(res[1], m_size.y) || !count(res[0], m_size.z))
+            return fail("Grid/resolution must be positive counts up to " + std::to_string(kMaxAxis));
         const Node *xr = root.child("XRay");
         const Node *srcs = xr ? xr->child("sources") : nullptr;
         if (srcs == nullptr || srcs->children.empty()) return fail("XRay/sources missing or empty");
@@ -367,8 +407,9 @@ private:
             return fail("Camera/pixelWidth missing, unreadable or zero");
         if (!kvxml::number(cam->child("pixelHeight"), ph) || static_cast<float>(ph) == 0.f)
             return fail("Camera/pixelHeight missing, unreadable or zero");
-        const Size2D det_px{static_cast<int>(static_cast<float>(pw)), static_cast<int>(static_cast<float>(ph))};
-        if (det_px.x <= 0 || det_px.y <= 0) return fail("Camera pixel counts must be positive");
+        Size2D det_px{0, 0};
+        if (!count(pw, det_px.x) || !count(ph, det_px.y))
+            return fail("Camera pixel counts must be positive counts up to " + std::to_string(kMaxAxis));
         m_pixel = {static_cast<float>(tw) / static_cast<float>(det_px.x),
                    static_cast<float>(th) / static_cast<float>(det_px.y)};
         const Node *refs = cam->child("references");
@@ -391,10 +432,12 @@ private:
             if (w.size() < 6) return fail("a Radios/rois entry is unreadable");
             int cur[4];
             try {
-                cur[0] = static_cast<int>(std::stod(w[0]));
-                cur[1] = static_cast<int>(std::stod(w[1]));
-                cur[2] = static_cast<int>(std::stod(w[4]));
-                cur[3] = static_cast<int>(std::stod(w[5]));
+                const size_t idx[4] = {0, 1, 4, 5};
+                for (int q = 0; q < 4; ++q) {
+                    const double d = std::stod(w[idx[q]]);
+                    if (!(d > -1e9 && d < 1e9)) return fail("a Radios/rois entry is out of range");
+                    cur[q] = static_cast<int>(d);
+                }
             } catch (const std::exception &) {
                 return fail("a Radios/rois entry is unreadable");
             }
@@ -417,9 +460,26 @@ private:
             for (int k = 0; k < bl[1]; ++k) y += m_pixel.y;
             m_roiBL.push_back({x, y});
         }
+        // every position, spacing and pitch must be a finite float; spacings
+        // and pitches positive
+        auto fin = [](float a) { return std::isfinite(a); };
+        if (!fin(m_fulcrum.x) || !fin(m_fulcrum.y) || !fin(m_fulcrum.z) || !fin(m_detZ))
+            return fail("non-finite fulcrum or detector position");
+        if (!(fin(m_spacing.x) && fin(m_spacing.y) && fin(m_spacing.z) && m_spacing.x > 0.f && m_spacing.y > 0.f &&
+              m_spacing.z > 0.f))
+            return fail("Grid/scale must be positive finite spacings");
+        if (!(fin(m_pixel.x) && fin(m_pixel.y) && m_pixel.x > 0.f && m_pixel.y > 0.f))
+            return fail("Camera extent / pixel count must give a positive finite pitch");
+        for (const auto &s : sources)
+            if (!fin(s.x) || !fin(s.y) || !fin(s.z)) return fail("non-finite source position");
+        for (const auto &r : m_roiBL)
+            if (!fin(r.x) || !fin(r.y)) return fail("non-finite detector reference");
         set_sources(sources);
         return true;
     }
+
+    // largest voxel or pixel count per axis read from a file
+    static constexpr int kMaxAxis = 1 << 20;
 
 public:
 

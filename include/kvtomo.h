@@ -156,7 +156,9 @@ kv_status kv_shift_and_add(kv_plan *plan, const float *projections, float *slice
 kv_status kv_fbp(kv_plan *plan, const float *projections, float *volume, int32_t half_taps, kv_mem mem);
 /* Host-only: the integer row shift of every (slice, view) pair that
  * kv_shift_and_add applies, [nz][n_views], computed without a device.
- * Replaces the shift loop of recons::ShiftAndAdd, Reconstructors.h:308-331. */
+ * Replaces the shift loop of recons::ShiftAndAdd, Reconstructors.h:308-331.
+ * Values are the rule's own, limited to +-2^30; non-finite geometry values
+ * are refused (KV_ERR_INVALID_ARG / KV_ERR_NUMERIC). */
 kv_status kv_shift_and_add_shifts(const kv_geometry *geom, kv_family family, int32_t *shifts);
 /* Fill `volume` with the uniform initial estimate 1.0 (PhantomMaker(vol,1.f)). */
 kv_status kv_uniform_volume(kv_plan *plan, float *volume, kv_mem mem);

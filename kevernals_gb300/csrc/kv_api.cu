@@ -84,6 +84,29 @@ kv_status ensure_sens(kv_plan *plan) {
     return KV_OK;
 }
 
+// The geometry's values, beyond the sizes: positive finite spacings and
+// pitches, a finite fulcrum, finite source and detector positions.
+kv_status check_geometry_values(kv_ctx *ctx, const kv_geometry &g) {
+    auto pos = [](float v) { return std::isfinite(v) && v > 0.f; };
+    if (!pos(g.dx) || !pos(g.dy) || !pos(g.dz) || !pos(g.du) || !pos(g.dv))
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "spacings must be positive and finite");
+    if (!std::isfinite(g.fulcrum_z)) return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite fulcrum height");
+    for (int i = 0; i < 3 * g.n_views; ++i)
+        if (!std::isfinite(g.src[i]) || !std::isfinite(g.det_origin[i]))
+            return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite source / detector position");
+    return KV_OK;
+}
+
+// A row shift (after the rule's own rounding or truncation) as an int32,
+// limited to +-limit so that the conversion is defined.
+constexpr int32_t kMaxShift = 1 << 30;
+template <typename T>
+int32_t stored_shift(T t, int32_t limit) {
+    if (t >= (T)limit) return limit;
+    if (t <= -(T)limit) return -limit;
+    return (int32_t)t;
+}
+
 // Integer row shifts of shift-and-add, one per (slice, view).
 // rule RC follows recons::ShiftAndAdd literally (Reconstructors.h:287-331);
 // rule EXACT uses heights above the detector plane and detector pixels.
@@ -91,6 +114,8 @@ kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_
     const int P = g.n_views, nz = g.nz;
     if (nz <= 1) return kv_fail(ctx, KV_ERR_GEOMETRY, "shift-and-add needs at least 2 slices (got %d)", nz);
     if (P <= 1) return kv_fail(ctx, KV_ERR_GEOMETRY, "shift-and-add needs at least 2 projections (got %d)", P);
+    if (g.nv <= 0) return kv_fail(ctx, KV_ERR_INVALID_ARG, "sizes must be positive");
+    KV_TRY(check_geometry_values(ctx, g));
     // common source z (TomoTable: float mean) and detector z (double sum, float mean)
     float src_z = 0.f;
     for (int i = 0; i < P; ++i) src_z += g.src[3 * i + 2];
@@ -115,7 +140,9 @@ kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_
             const float coeff = sid / (sid - z) - mf;
             for (int i = 0; i < P; ++i) {
                 const float t = g.src[3 * i + 1] * coeff;
-                sh[(size_t)k * P + i] = (int32_t)(t / g.dy);
+                const float q = t / g.dy;
+                if (std::isnan(q)) return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite shift at slice %d", k);
+                sh[(size_t)k * P + i] = stored_shift(std::trunc(q), kMaxShift);
             }
         }
     } else {
@@ -127,8 +154,11 @@ kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_
             const double hz = -0.5 * nz * (double)g.dz + (k + 0.5) * (double)g.dz - (double)det_z;
             if (std::fabs(sid - hz) < 1e-9 * std::fabs(sid)) return kv_fail(ctx, KV_ERR_GEOMETRY, "slice %d at the source height", k);
             const double mz = sid / (sid - hz);
-            for (int i = 0; i < P; ++i)
-                sh[(size_t)k * P + i] = (int32_t)std::lround((double)g.src[3 * i + 1] * (mz - mf) / (double)g.dv);
+            for (int i = 0; i < P; ++i) {
+                const double q = (double)g.src[3 * i + 1] * (mz - mf) / (double)g.dv;
+                if (std::isnan(q)) return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite shift at slice %d", k);
+                sh[(size_t)k * P + i] = stored_shift(std::round(q), kMaxShift);
+            }
         }
     }
     return KV_OK;
@@ -357,10 +387,9 @@ extern "C" kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *g, kv_family
     *out = nullptr;
     if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || g->nu <= 0 || g->nv <= 0 || g->n_views <= 0)
         return kv_fail(ctx, KV_ERR_INVALID_ARG, "sizes must be positive");
-    if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->du > 0) || !(g->dv > 0))
-        return kv_fail(ctx, KV_ERR_INVALID_ARG, "spacings must be positive");
     if (g->src == nullptr || g->det_origin == nullptr)
         return kv_fail(ctx, KV_ERR_INVALID_ARG, "null source / detector array");
+    KV_TRY(check_geometry_values(ctx, *g));
     if ((size_t)g->nx * g->ny >= (1ull << 31) || (size_t)g->nu * g->nv >= (1ull << 31))
         return kv_fail(ctx, KV_ERR_INVALID_ARG, "slice or detector larger than 2^31 elements");
     if (family != KV_FAMILY_RC && family != KV_FAMILY_EXACT)
@@ -369,9 +398,6 @@ extern "C" kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *g, kv_family
         return kv_fail(ctx, KV_ERR_INVALID_ARG, "bad storage");
     if (family == KV_FAMILY_RC && storage != KV_STORAGE_F32)
         return kv_fail(ctx, KV_ERR_UNSUPPORTED, "the reference-compatible family is FP32 only");
-    for (int i = 0; i < 3 * g->n_views; ++i)
-        if (!std::isfinite(g->src[i]) || !std::isfinite(g->det_origin[i]))
-            return kv_fail(ctx, KV_ERR_NUMERIC, "non-finite source / detector position");
     KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
     kv_plan *plan = new (std::nothrow) kv_plan;
     if (plan == nullptr) return KV_ERR_OOM;
@@ -580,6 +606,10 @@ extern "C" kv_status kv_shift_and_add(kv_plan *plan, const float *proj, float *s
     KV_TRY(check_common(plan, proj, slices, mem));
     std::vector<int32_t> sh((size_t)plan->g.nz * plan->g.n_views);
     KV_TRY(saa_shifts(plan->ctx, plan->g, plan->family, sh.data()));
+    // a shift of nv rows or more moves every row off the detector (zero
+    // padding): +-nv gives the same sum and keeps the kernel's row index
+    // v + shift far from overflow
+    for (int32_t &s : sh) s = std::min(std::max(s, -plan->g.nv), plan->g.nv);
     const size_t nout = (size_t)plan->g.nz * plan->g.nv * plan->g.nu;
     KV_TRY(ensure(plan->ctx, &plan->d_shift, sh.size() * sizeof(int32_t)));
     KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(plan->d_shift, sh.data(), sh.size() * sizeof(int32_t),

@@ -4,11 +4,21 @@
 
 #include "kevernals_tomo.hpp"
 
+// a string as the body of a JSON string literal
+static std::string json_escape(const std::string &v) {
+    std::string out;
+    for (char c : v) {
+        if (c == '"' || c == '\\') out += '\\';
+        out += c;
+    }
+    return out;
+}
+
 int main(int argc, char **argv) {
     if (argc < 2) return 2;
     TomoGeometry geo{std::string(argv[1])};
     if (!geo.IsValid()) {
-        std::printf("{\"valid\": false, \"error\": \"%s\"}\n", geo.ErrorMessage().c_str());
+        std::printf("{\"valid\": false, \"error\": \"%s\"}\n", json_escape(geo.ErrorMessage()).c_str());
         return 0;
     }
     const auto f = geo.flatten();

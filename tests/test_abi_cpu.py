@@ -72,6 +72,29 @@ def test_shift_rule_rejects_degenerate_geometry(lib):
         engine.shift_and_add_shifts(g, "exact")
 
 
+def test_shift_rule_refuses_non_finite_values(lib):
+    import dataclasses
+    g = linear_sweep(8, 8, 4, 0.5, 0.5, 1.0, 3, 8, 8, 0.5, 0.5, 10.0)
+    bad_src = g.src.copy()
+    bad_src[1, 1] = np.nan
+    for bad in (dataclasses.replace(g, fulcrum_z=float("nan")), dataclasses.replace(g, dy=float("inf")),
+                dataclasses.replace(g, dv=0.0), dataclasses.replace(g, src=bad_src)):
+        for family in ("rc", "exact"):
+            with pytest.raises(_lib.KvError):
+                engine.shift_and_add_shifts(bad, family)
+
+
+@pytest.mark.parametrize("family,rule", [("rc", 0), ("exact", 1)])
+def test_shift_rule_keeps_shifts_beyond_the_detector(lib, family, rule):
+    """A detector of 4 rows under a +-25 deg sweep: most shifts exceed the
+    row count and are returned as the rule gives them (the device copy
+    limits them to +-nv, the same sum)."""
+    g = linear_sweep(32, 32, 17, 0.4, 0.4, 2.5, 9, 64, 4, 0.3, 0.3, 25.0)
+    ref = O.saa_shifts(g, rule)
+    assert (np.abs(ref) > g.nv).any()
+    assert np.array_equal(engine.shift_and_add_shifts(g, family), ref)
+
+
 def test_cpp_dropin_compiles_and_links(lib, tmp_path):
     """The C++ drop-in headers (kevernals_tomo.hpp, kevernals_dicom.hpp,
     kevernals_output.hpp) compile with warnings as errors and the drop-in

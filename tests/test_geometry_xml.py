@@ -117,3 +117,68 @@ def test_xml_geometry_rejects_bad_files(dumper, tmp_path):
     assert not got["valid"] and "XML" in got["error"]
     got = read(dumper, str(tmp_path / "missing.xml"))
     assert not got["valid"] and "cannot open" in got["error"]
+
+
+def test_xml_geometry_rejects_out_of_range_values(dumper, tmp_path):
+    """Values a float cannot hold, non-positive counts and spacings, and
+    non-finite positions are refused with a reason (not passed on)."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path)
+    txt = open(path).read()
+    cases = [("<scale>1.0 0.5 0.5</scale>", "<scale>1.0 1e40 0.5</scale>", "Grid/scale"),
+             ("<scale>1.0 0.5 0.5</scale>", "<scale>1.0 -0.5 0.5</scale>", "Grid/scale"),
+             ("<resolution>16 64 48</resolution>", "<resolution>16 0 48</resolution>", "Grid/resolution"),
+             ("<resolution>16 64 48</resolution>", "<resolution>16 1e12 48</resolution>", "Grid/resolution"),
+             ("<pixelWidth>100</pixelWidth>", "<pixelWidth>nan</pixelWidth>", "pixel counts"),
+             ("<totalWidth>40</totalWidth>", "<totalWidth>-40</totalWidth>", "pitch"),
+             ("<source>10.0 -130.0 940.0</source>", "<source>10.0 -130.0 inf</source>", "source"),
+             ("<center>10.0 20.0 190.0</center>", "<center>10.0 20.0 1e39</center>", "fulcrum"),
+             ("<roi>10 20 0 0 89 79</roi>", "<roi>10 20 0 0 1e30 79</roi>", "Radios/rois")]
+    for old, new, why in cases:
+        assert old in txt, old
+        with open(path, "w") as fh:
+            fh.write(txt.replace(old, new, 1))
+        got = read(dumper, path)
+        assert not got["valid"] and why in got["error"], (new, got)
+
+
+def test_xml_reader_survives_hostile_files(tmp_path):
+    """Truncations, seeded byte corruptions and out-of-range numbers of a good
+    file, deep nesting and an entity flood, read by the dump tool built with
+    AddressSanitizer and UBSan (plain when the compiler lacks them): each
+    ends within a time limit with a result or a printable error."""
+    import re
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "geometry_xml_dump")
+    base = ["g++", "-std=c++17", "-O1", "-g", "-I", os.path.join(ROOT, "include"),
+            os.path.join(ROOT, "tests", "cpp", "geometry_xml_dump.cpp"), "-o", exe]
+    if subprocess.run(base + ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined"],
+                      capture_output=True).returncode != 0:
+        subprocess.run(base, check=True)
+    good = str(tmp_path / "good.xml")
+    write_xml(good)
+    raw = open(good, "rb").read()
+    rng = np.random.default_rng(2)
+    variants = [raw[:c] for c in range(0, len(raw), 11)]
+    for _ in range(80):
+        b = bytearray(raw)
+        for pos in rng.integers(0, len(raw), size=rng.integers(1, 4)):
+            b[pos] = rng.integers(0, 256)
+        variants.append(bytes(b))
+    txt = raw.decode()
+    spans = [m.span() for m in re.finditer(r"-?\d+(\.\d+)?", txt)]
+    for bad in ("1e40", "nan", "-inf", "99999999999", "-2147483649", ""):
+        for k in rng.choice(len(spans), 6, replace=False):
+            a, b = spans[k]
+            variants.append((txt[:a] + bad + txt[b:]).encode())
+    variants.append(("<Geometry>" + "<a>" * 100000 + "</a>" * 100000 + "</Geometry>").encode())
+    variants.append(("<Geometry><Rotation><center>" + "&amp;" * 200000 + "</center></Rotation></Geometry>").encode())
+    path = str(tmp_path / "v.xml")
+    for v in variants:
+        with open(path, "wb") as fh:
+            fh.write(v)
+        r = subprocess.run([exe, path], capture_output=True, timeout=20)
+        assert r.returncode == 0 and b"ERROR" not in r.stderr and b"runtime error" not in r.stderr, r.stderr[-1500:]
+        out = json.loads(r.stdout.decode("ascii"))
+        assert out["valid"] or out["error"]
