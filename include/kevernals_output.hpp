@@ -37,20 +37,21 @@ using ImageU16Ptr = std::shared_ptr<ImageU16>;
 
 // out = clamp((x + 0) * (65535 - 1) / max(x), 0, 65535), truncated to
 // unsigned short (vtkImageShiftScale without rounding); max(x) is the
-// volume's largest value.  A volume whose maximum is not positive gives zeros.
+// volume's largest finite value.  A volume whose maximum is not positive
+// gives zeros; NaN voxels give 0 and +inf voxels 65535.
 inline ImageU16Ptr RescaleToUInt16(const ImageDataPtr &in) {
     auto out = std::make_shared<ImageU16>();
     const int *d = in->GetDimensions();
     for (int i = 0; i < 3; ++i) out->dims[i] = d[i];
     out->data.assign(in->size(), 0);
     double mx = -HUGE_VAL;
-    for (size_t i = 0; i < in->size(); ++i) mx = std::max(mx, (double)in->data()[i]);
+    for (size_t i = 0; i < in->size(); ++i)
+        if (std::isfinite(in->data()[i])) mx = std::max(mx, (double)in->data()[i]);
     if (!(mx > 0.0)) return out;
     const double scale = (double)(USHRT_MAX - 1) / mx;
     for (size_t i = 0; i < in->size(); ++i) {
-        double v = (double)in->data()[i] * scale;
-        v = std::min(std::max(v, 0.0), (double)USHRT_MAX);
-        out->data[i] = (uint16_t)v;
+        const double v = (double)in->data()[i] * scale;
+        out->data[i] = v > 0.0 ? (uint16_t)std::min(v, (double)USHRT_MAX) : (uint16_t)0;   // NaN -> 0
     }
     return out;
 }

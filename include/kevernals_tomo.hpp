@@ -621,13 +621,17 @@ namespace kvtomo_detail {
 // per z slice; samples of `bytes` bytes, SampleFormat 1 (unsigned) or 3 (IEEE).
 inline bool write_tiff_pages(const std::string &path, int w, int h, int pages, int bytes, int sample_format,
                              const uint8_t *data) {
+    const int ntags = 11;
+    const uint32_t ifd_bytes = 2 + ntags * 12 + 4;
+    // classic TIFF: 32-bit offsets, so the whole file must stay below 4 GiB
+    if (w <= 0 || h <= 0 || pages <= 0 || data == nullptr) return false;
+    const uint64_t total = 8 + (uint64_t)pages * (ifd_bytes + (uint64_t)w * h * bytes);
+    if (total >= (1ull << 32)) return false;
+    const uint32_t page_bytes = (uint32_t)w * h * bytes;
     std::ofstream f(path, std::ios::binary);
     if (!f) return false;
     auto put16 = [&](uint16_t v) { f.put((char)(v & 0xFF)); f.put((char)(v >> 8)); };
     auto put32 = [&](uint32_t v) { for (int i = 0; i < 4; ++i) f.put((char)((v >> (8 * i)) & 0xFF)); };
-    const uint32_t page_bytes = (uint32_t)w * h * bytes;
-    const int ntags = 11;
-    const uint32_t ifd_bytes = 2 + ntags * 12 + 4;
     f.write("II", 2);
     put16(42);
     put32(8);                                    // first IFD right after the header

@@ -106,10 +106,21 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
     root = os.path.dirname(os.path.dirname(__file__))
     so = os.path.dirname(build.build())
     src = tmp_path / "all_headers.cpp"
+    # the TIFF writer refuses a file beyond classic TIFF's 32-bit offsets
+    # (without reading the data) and writes a small one
     src.write_text('#include "kevernals_tomo.hpp"\n#include "kevernals_dicom.hpp"\n'
-                   '#include "kevernals_output.hpp"\nint main() { return 0; }\n')
+                   '#include "kevernals_output.hpp"\n'
+                   'int main(int, char **argv) {\n'
+                   '    const uint8_t px[4] = {0, 0, 128, 63};\n'
+                   '    if (kvtomo_detail::write_tiff_pages(argv[1], 70000, 70000, 1, 4, 3, px)) return 1;\n'
+                   '    if (!kvtomo_detail::write_tiff_pages(argv[1], 1, 1, 1, 4, 3, px)) return 2;\n'
+                   '    return 0;\n}\n')
     for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp")):
         r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I",
                             os.path.join(root, "include"), f, "-o", str(tmp_path / "a.out"), "-L", so,
                             "-lkvtomo", "-Wl,-rpath," + so], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr[-3000:]
+        if f == str(src):
+            tif = tmp_path / "one.tif"
+            assert subprocess.run([str(tmp_path / "a.out"), str(tif)]).returncode == 0
+            assert tif.stat().st_size == 8 + 2 + 11 * 12 + 4 + 4

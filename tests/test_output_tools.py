@@ -100,3 +100,19 @@ def test_tiff_rescale_and_histogram_tools(tool, tmp_path):
     assert np.array_equal(half, hist_match(exp, u16, nx * ny))
     # uniformisation spreads the grey levels over the whole range
     assert int(uni.max()) > 60000 and np.count_nonzero(uni[0, :4, :5]) == 0
+
+
+def test_rescale_handles_non_finite_voxels(tool, tmp_path):
+    """NaN voxels map to 0 and +-inf to the ends of the range; the scale comes
+    from the largest finite voxel."""
+    nx, ny, nz = 8, 4, 2
+    vol = np.linspace(0.0, 2.0, nx * ny * nz, dtype=np.float32).reshape(nz, ny, nx)
+    vol[0, 0, :3] = [np.nan, np.inf, -np.inf]
+    raw = tmp_path / "vol.raw"
+    vol.tofile(raw)
+    subprocess.run([tool, str(raw), str(nx), str(ny), str(nz), str(tmp_path)], check=True)
+    u16 = np.fromfile(tmp_path / "u16.raw", np.uint16).reshape(nz, ny, nx)
+    assert list(u16[0, 0, :3]) == [0, 65535, 0]
+    finite = np.isfinite(vol)
+    exp = rescale_u16(np.where(finite, vol, 0.0).astype(np.float32))
+    assert np.array_equal(u16[finite], exp[finite])
