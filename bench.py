@@ -307,6 +307,25 @@ def time_to_residual(ctx, g, cfg, rank, plain_iters=50):
             "speedup": r["speedup"], "checkpoint": os.path.relpath(WEIGHTS, ROOT)}
 
 
+def gather_rate(kernel, g, sv, sp, avg_ms):
+    """The projector's gather work, beside the compulsory bytes: one element
+    read per Siddon segment (a voxel for a forward walk, a ray value for the
+    EXACT gather backprojector; the RC backprojector scans pixel windows
+    instead and gets no figure); segments counted from the geometry on every
+    8th detector row and column and scaled to all rays.  Mostly served by
+    L1 / L2, so it is a rate of work, not of DRAM traffic."""
+    try:
+        if kernel not in ("exact_fwd", "exact_back", "rc_fwd"):
+            return {}
+        from kevernals_gb300.geometry import siddon_segments
+        seg = siddon_segments(g, 8)
+        elem = sv if kernel.endswith("fwd") else sp
+        return {"segments_per_launch": seg, "gather_bytes": elem * seg,
+                "gather_gbs": elem * seg / (avg_ms * 1e-3) / 1e9}
+    except Exception as e:          # a missing figure must not cost the line
+        return {"gather_unavailable": f"{type(e).__name__}: {e}"}
+
+
 def max_over_ranks(ms, world, device):
     """The slowest rank's time: replicas finish when the last one does.  One
     all-reduce (MAX) over the process group; the identity on one rank."""
@@ -387,6 +406,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
             roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak, "peak_source": src, "algorithmic_bytes": byt,
                     "traffic": committed_traffic(dom, args.workload), "avg_ms": tot / n}
+            roof.update(gather_rate(dom, g, sv, sp, tot / n))
 
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None

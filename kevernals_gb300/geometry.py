@@ -123,3 +123,55 @@ def _half_angle(g: Geometry) -> float:
     sid = float(g.src[0, 2]) + zc
     sod = sid - (float(g.fulcrum_z) + zc)
     return math.degrees(math.atan(abs(float(g.src[:, 1].max())) / sod))
+
+
+# ---- Siddon segment counts (the gather work of one projector pass) -------
+
+def segments_per_ray(g: Geometry, view: int, uc, vc) -> np.ndarray:
+    """Voxels with a positive intersection length along the rays of `view`
+    through detector positions (uc, vc) in pixels (pixel centres are
+    u + 0.5, v + 0.5; the arrays broadcast).  Between the box entry and exit
+    a ray visits 1 + the x, y and z planes it crosses; a ray through an edge
+    or a corner of the grid (a set of measure zero) is counted one voxel
+    high.  Rays that miss the box count 0."""
+    s = g.src[view].astype(np.float64)
+    o = g.det_origin[view].astype(np.float64)
+    uc, vc = np.broadcast_arrays(np.asarray(uc, np.float64), np.asarray(vc, np.float64))
+    d = (o[0] + uc * g.du - s[0], o[1] + vc * g.dv - s[1], np.full(uc.shape, o[2] - s[2]))
+    n = (g.nx, g.ny, g.nz)
+    sp = (g.dx, g.dy, g.dz)
+    tin = np.zeros(uc.shape)
+    tout = np.ones(uc.shape)
+    for a in range(3):
+        h = 0.5 * n[a] * sp[a]
+        da = d[a]
+        moving = da != 0.0
+        safe = np.where(moving, da, 1.0)
+        t_lo, t_hi = (-h - s[a]) / safe, (h - s[a]) / safe
+        lo = np.where(moving, np.minimum(t_lo, t_hi), np.where(abs(s[a]) < h, -np.inf, np.inf))
+        hi = np.where(moving, np.maximum(t_lo, t_hi), np.where(abs(s[a]) < h, np.inf, -np.inf))
+        tin = np.maximum(tin, lo)
+        tout = np.minimum(tout, hi)
+    hit = tout > tin
+    eps = 1e-9 * np.where(hit, tout - tin, 0.0)
+    te, tx = tin + eps, tout - eps
+    count = np.ones(uc.shape)
+    for a in range(3):
+        h = 0.5 * n[a] * sp[a]
+        ie = np.floor((s[a] + te * d[a] + h) / sp[a])
+        ix = np.floor((s[a] + tx * d[a] + h) / sp[a])
+        count += np.abs(ix - ie)
+    return np.where(hit, count, 0.0)
+
+
+def siddon_segments(g: Geometry, stride: int = 1) -> float:
+    """Siddon segments -- (ray, voxel) pairs with a positive intersection
+    length -- of one forward projection (equally, of its transpose), from the
+    rays of every `stride`-th detector column and row of every view, scaled
+    to all rays when stride > 1."""
+    us = np.arange(stride // 2, g.nu, stride) + 0.5     # the middle column of each block
+    vs = np.arange(stride // 2, g.nv, stride) + 0.5
+    total = 0.0
+    for p in range(g.n_views):
+        total += float(segments_per_ray(g, p, us[None, :], vs[:, None]).sum())
+    return total * (g.nu * g.nv) / (len(us) * len(vs))

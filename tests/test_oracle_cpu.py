@@ -175,6 +175,26 @@ def test_fbp_ramp_known_answers():
     assert np.allclose(O.ramp_filter_v(2.0 * a - b, K), 2.0 * O.ramp_filter_v(a, K) - O.ramp_filter_v(b, K))
 
 
+def test_siddon_segment_count_matches_oracle():
+    """geometry.segments_per_ray -- the gather work the benchmark reports --
+    equals the number of voxels the FP64 oracle's transpose of a single ray
+    touches, on random rays of three geometries."""
+    from kevernals_gb300.geometry import segments_per_ray, siddon_segments
+    rng = np.random.default_rng(0)
+    for g in (linear_sweep(40, 36, 12, 0.5, 0.5, 1.0, 5, 48, 44, 0.4, 0.4, 15.0),
+              linear_sweep(33, 29, 7, 0.7, 0.45, 1.3, 4, 37, 41, 0.55, 0.35, 22.0),
+              linear_sweep(64, 64, 16, 0.4, 0.4, 2.5, 9, 96, 96, 0.2, 0.2, 17.5)):
+        for r in rng.integers(0, g.n_rays, 100):
+            p, rem = divmod(int(r), g.nu * g.nv)
+            v, u = divmod(rem, g.nu)
+            vol = np.zeros(g.n_voxels)
+            O.exact_back_rays(g, np.ones(1), np.array([r]), vol)
+            assert int(segments_per_ray(g, p, u + 0.5, v + 0.5)) == np.count_nonzero(vol)
+        # the sampled total extrapolates the full one closely
+        full = siddon_segments(g, 1)
+        assert abs(siddon_segments(g, 4) - full) <= 0.02 * full
+
+
 def test_splitmix64_known_values():
     # first outputs of splitmix64 seeded with 0 (published reference sequence)
     r = ph.SplitMix64(0)
