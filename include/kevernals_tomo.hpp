@@ -26,7 +26,9 @@
 //     without `inline`).
 #pragma once
 
+#include <algorithm>
 #include <cctype>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -61,6 +63,7 @@ struct VoxelSpacing {
     float x = 0.f, y = 0.f, z = 0.f;
 };
 using WSize3D = Position3D;
+using WSize2D = Position2D;
 
 // ---------------------------------------------------------------- errors
 
@@ -410,8 +413,8 @@ private:
         Size2D det_px{0, 0};
         if (!count(pw, det_px.x) || !count(ph, det_px.y))
             return fail("Camera pixel counts must be positive counts up to " + std::to_string(kMaxAxis));
-        m_pixel = {static_cast<float>(tw) / static_cast<float>(det_px.x),
-                   static_cast<float>(th) / static_cast<float>(det_px.y)};
+        m_detWSize = {static_cast<float>(tw), static_cast<float>(th)};
+        m_pixel = {m_detWSize.x / static_cast<float>(det_px.x), m_detWSize.y / static_cast<float>(det_px.y)};
         const Node *refs = cam->child("references");
         if (refs == nullptr || refs->children.empty()) return fail("Camera/references missing or empty");
         std::vector<Position2D> det_bl;
@@ -475,6 +478,7 @@ private:
         for (const auto &r : m_roiBL)
             if (!fin(r.x) || !fin(r.y)) return fail("non-finite detector reference");
         set_sources(sources);
+        m_roiPixel = m_pixel;
         return true;
     }
 
@@ -492,11 +496,34 @@ public:
                  const std::vector<Position2D> &roiBottomLeft, float detectorZ, Size2D roiSize,
                  PixelSpacing pixelSpacing, WSize3D fulcrum = {})
         : m_size(volumeSize), m_spacing(spacing), m_roiBL(roiBottomLeft), m_roiSize(roiSize),
-          m_pixel(pixelSpacing), m_fulcrum(fulcrum), m_detZ(detectorZ) {
+          m_pixel(pixelSpacing), m_roiPixel(pixelSpacing), m_fulcrum(fulcrum), m_detZ(detectorZ) {
         if (sources.size() != roiBottomLeft.size() || sources.empty())
             throw std::invalid_argument("TomoGeometry: one source and one ROI origin per view");
         set_sources(sources);
+        // built from values, the detector is taken to be the ROI
+        m_detWSize = {pixelSpacing.x * static_cast<float>(roiSize.x), pixelSpacing.y * static_cast<float>(roiSize.y)};
         m_valid = true;
+    }
+
+    // TomoGeometry::PerformCheatingAdaptationsForDemonstration
+    // (TomoGeometry.cpp:593-611), which the reference's reconstruction main
+    // applies after reading a geometry file.  It drops the listed views
+    // (indices taken in decreasing order, out-of-range ones skipped; the
+    // common source x and z stay the means over all the views read), gives
+    // the volume 100 slices of the same spacing, and resamples the detector
+    // and its ROI to 3048 x 3048 pixels: the detector pitch, the one the
+    // projector uses, becomes the detector's width / 3048, while the ROI
+    // corners and the ROI's own pitch keep their values.
+    void PerformCheatingAdaptationsForDemonstration(const std::vector<int> &p_dataIndicesToRemove) {
+        auto indices = p_dataIndicesToRemove;
+        std::sort(indices.begin(), indices.end(), std::greater<int>());
+        for (int i : indices)
+            if (i >= 0 && i < static_cast<int>(m_srcY.size())) m_srcY.erase(m_srcY.begin() + i);
+        for (int i : indices)
+            if (i >= 0 && i < static_cast<int>(m_roiBL.size())) m_roiBL.erase(m_roiBL.begin() + i);
+        m_size.z = 100;
+        m_pixel = {m_detWSize.x / 3048.f, m_detWSize.y / 3048.f};
+        m_roiSize = {3048, 3048};
     }
     bool IsValid() const { return m_valid; }
     const std::string &ErrorMessage() const { return m_error; }
@@ -516,7 +543,7 @@ public:
     Size2D GetProjectionROIsBLPixelPositionOnDetector() const { return m_roiBLPixel; }
     void SetProjectionROIsBLPixelPositionOnDetector(Size2D p) { m_roiBLPixel = p; }
     PixelSpacing projectionsPixelSpacing() const { return m_pixel; }
-    PixelSpacing projectionsRoisPixelSpacing() const { return m_pixel; }
+    PixelSpacing projectionsRoisPixelSpacing() const { return m_roiPixel; }
     Size3D volumeSize3D() const { return m_size; }
     VoxelSpacing volumeVoxelSpacing() const { return m_spacing; }
     Position3D volumeBLF() const {
@@ -570,7 +597,9 @@ private:
     std::vector<Position2D> m_roiBL;
     Size2D m_roiSize;
     Size2D m_roiBLPixel;
-    PixelSpacing m_pixel;
+    PixelSpacing m_pixel;     // detector pitch (what the projector uses)
+    PixelSpacing m_roiPixel;  // the ROI set's own pitch
+    WSize2D m_detWSize;       // detector extent (mm)
     WSize3D m_fulcrum;
     float m_detZ = 0.f;
     bool m_valid = false;

@@ -1,6 +1,11 @@
 // Reads a geometry file with the drop-in header's TomoGeometry(path) and
-// prints the flattened description the kernels receive, as JSON.
+// prints the flattened description the kernels receive, as JSON.  With
+// "adapt i j ..." after the path it first applies
+// PerformCheatingAdaptationsForDemonstration({i, j, ...}).
 #include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
 
 #include "kevernals_tomo.hpp"
 
@@ -20,6 +25,11 @@ int main(int argc, char **argv) {
     if (!geo.IsValid()) {
         std::printf("{\"valid\": false, \"error\": \"%s\"}\n", json_escape(geo.ErrorMessage()).c_str());
         return 0;
+    }
+    if (argc > 2 && std::string(argv[2]) == "adapt") {
+        std::vector<int> remove;
+        for (int i = 3; i < argc; ++i) remove.push_back(std::atoi(argv[i]));
+        geo.PerformCheatingAdaptationsForDemonstration(remove);
     }
     const auto f = geo.flatten();
     const kv_geometry &g = f->g;

@@ -182,3 +182,29 @@ def test_xml_reader_survives_hostile_files(tmp_path):
         assert r.returncode == 0 and b"ERROR" not in r.stderr and b"runtime error" not in r.stderr, r.stderr[-1500:]
         out = json.loads(r.stdout.decode("ascii"))
         assert out["valid"] or out["error"]
+
+
+def test_demonstration_adaptations(dumper, tmp_path):
+    """PerformCheatingAdaptationsForDemonstration (TomoGeometry.cpp:593-611),
+    as mainReconstruct.cpp applies it.  Indices {3, 0, 9, 3} of 5 views,
+    erased in decreasing order as the reference does: 9 is out of range, the
+    repeated 3 erases the view that moved into that slot (view 4), so views
+    1 and 2 remain.  100 slices, a 3048 x 3048 ROI whose pitch is the
+    detector width / 3048; the common source x / z and the remaining ROI
+    corners keep their values."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path)
+    before = read(dumper, path)
+    out = subprocess.run([dumper, path, "adapt", "3", "0", "9", "3"], check=True, capture_output=True,
+                         text=True).stdout
+    after = json.loads(out)
+    assert after["valid"] and after["views"] == 2
+    assert after["n"] == [before["n"][0], before["n"][1], 100] and after["d"] == before["d"]
+    assert after["det"] == [3048, 3048]
+    assert np.float32(after["pitch"][0]) == f32(f32(40) / f32(3048))
+    assert np.float32(after["pitch"][1]) == f32(f32(30) / f32(3048))
+    keep = [1, 2]
+    src = np.asarray(before["src"], np.float32).reshape(-1, 3)
+    det = np.asarray(before["det_origin"], np.float32).reshape(-1, 3)
+    assert np.array_equal(np.asarray(after["src"], np.float32).reshape(-1, 3), src[keep])
+    assert np.array_equal(np.asarray(after["det_origin"], np.float32).reshape(-1, 3), det[keep])
