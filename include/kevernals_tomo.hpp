@@ -35,6 +35,7 @@
 #include <sstream>
 #include <memory>
 #include <optional>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <system_error>
@@ -107,6 +108,14 @@ template <> struct is_error_code_enum<ReconstructorsErrorCode> : public true_typ
 
 inline std::error_code make_error_code(ReconstructorsErrorCode e) {
     return {static_cast<int>(e), kvtomo_detail::reconstructors_category()};
+}
+
+// commons/PrintErrorCode.h: "<category>:<value> <message>. Details: <comment>"
+inline std::string PrintErrorCode(const std::error_code &p_errorCode,
+                                  const std::string &p_additionalComment = std::string("none.")) {
+    std::stringstream stream;
+    stream << p_errorCode << " " << p_errorCode.message() << ". Details: " << p_additionalComment;
+    return stream.str();
 }
 
 // Value-or-error, the subset of outcome::result the reference uses.
@@ -605,6 +614,25 @@ private:
     bool m_valid = false;
     std::string m_error;
 };
+
+// A readable summary under the reference printer's headings
+// (TomoGeometry.h:119-125): volume, projections, projections Rois, table.
+inline std::ostream &operator<<(std::ostream &os, TomoGeometry const &g) {
+    const auto n = g.volumeSize3D();
+    const auto d = g.volumeVoxelSpacing();
+    const auto roi = g.projectionsRoisSize();
+    const auto px = g.projectionsPixelSpacing();
+    os << "volume " << n.x << " x " << n.y << " x " << n.z << " voxels of " << d.x << " x " << d.y << " x " << d.z
+       << " mm, centred at the origin" << std::endl;
+    os << "projections: " << g.nbProjections() << " views, pixel pitch " << px.x << " x " << px.y << " mm" << std::endl;
+    os << "projections Rois: " << roi.x << " x " << roi.y << " pixels, bottom-left corners";
+    for (const auto &b : g.projectionsRoisBottomLeftPositions()) os << " (" << b.x << ", " << b.y << ")";
+    os << std::endl;
+    os << "table: sources x " << g.sourcesXCommonPosition() << ", z " << g.sourcesZCommonPosition() << ", y";
+    for (float y : g.sourcesYPositions()) os << " " << y;
+    os << "; detector z " << g.detectorsZCommonPosition() << std::endl;
+    return os;
+}
 
 // ---------------------------------------------------------------- engine
 

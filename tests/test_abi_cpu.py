@@ -114,6 +114,15 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
                    '    const uint8_t px[4] = {0, 0, 128, 63};\n'
                    '    if (kvtomo_detail::write_tiff_pages(argv[1], 70000, 70000, 1, 4, 3, px)) return 1;\n'
                    '    if (!kvtomo_detail::write_tiff_pages(argv[1], 1, 1, 1, 4, 3, px)) return 2;\n'
+                   '    Result<ImageDataPtr> r = ReconstructorsErrorCode::MLEM;\n'
+                   '    if (PrintErrorCode(r.error()) != "Reconstructors:4 MLEM reconstruction failed. Details: none.")\n'
+                   '        return 3;\n'
+                   '    TomoGeometry g({8, 8, 4}, {1.f, 1.f, 1.f}, {{0.f, -5.f, 100.f}, {0.f, 5.f, 100.f}},\n'
+                   '                   {{-4.f, -4.f}, {-4.f, -4.f}}, -10.f, {8, 8}, {1.f, 1.f});\n'
+                   '    std::ostringstream os;\n'
+                   '    os << g;\n'
+                   '    for (const char *h : {"volume ", "projections: ", "projections Rois: ", "table: "})\n'
+                   '        if (os.str().find(h) == std::string::npos) return 4;\n'
                    '    return 0;\n}\n')
     for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp")):
         r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I",
