@@ -124,7 +124,8 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
                    '    for (const char *h : {"volume ", "projections: ", "projections Rois: ", "table: "})\n'
                    '        if (os.str().find(h) == std::string::npos) return 4;\n'
                    '    return 0;\n}\n')
-    for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp")):
+    example = os.path.join(root, "tests", "cpp", "reconstruct_example.cpp")
+    for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp"), example):
         r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I",
                             os.path.join(root, "include"), f, "-o", str(tmp_path / "a.out"), "-L", so,
                             "-lkvtomo", "-Wl,-rpath," + so], capture_output=True, text=True)
@@ -133,3 +134,13 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
             tif = tmp_path / "one.tif"
             assert subprocess.run([str(tmp_path / "a.out"), str(tif)]).returncode == 0
             assert tif.stat().st_size == 8 + 2 + 11 * 12 + 4 + 4
+        if f == example:
+            # the reference main's flow: errors before any device work are reported, not fatal
+            from test_geometry_xml import write_xml
+            run = lambda *a: subprocess.run([str(tmp_path / "a.out"), *a], capture_output=True,  # noqa: E731
+                                            text=True)
+            r = run(str(tmp_path / "missing.xml"), str(tmp_path), str(tmp_path) + "/")
+            assert r.returncode == 1 and "invalid geometry: cannot open" in r.stdout
+            write_xml(str(tmp_path / "geo.xml"))
+            r = run(str(tmp_path / "geo.xml"), str(tmp_path / "no_series"), str(tmp_path) + "/")
+            assert r.returncode == 1 and "does not exist" in r.stdout and "projections Rois:" in r.stdout
