@@ -90,6 +90,35 @@ inline const std::error_category &reconstructors_category() {
     return c;
 }
 
+// n positions from `first` by repeated float addition of `step`
+inline std::vector<float> axis_positions(float first, float step, int n) {
+    std::vector<float> v(n > 0 ? n : 0);
+    if (n > 0) v[0] = first;
+    for (int i = 1; i < n; ++i) v[i] = v[i - 1] + step;
+    return v;
+}
+// per view: positions along x (or y) of its n pixels from the view's corner
+inline std::vector<std::vector<float>> view_positions(const std::vector<Position2D> &corners, bool x, float step,
+                                                      int n) {
+    std::vector<std::vector<float>> out;
+    for (const auto &c : corners) out.push_back(axis_positions(x ? c.x : c.y, step, n));
+    return out;
+}
+// every pixel of every view, views then rows then columns
+inline std::vector<Position2D> pixel_positions(const std::vector<std::vector<float>> &xs,
+                                               const std::vector<std::vector<float>> &ys) {
+    std::vector<Position2D> out;
+    for (size_t p = 0; p < xs.size(); ++p)
+        for (float y : ys[p])
+            for (float x : xs[p]) out.push_back({x, y});
+    return out;
+}
+inline std::vector<int> indices(size_t n) {
+    std::vector<int> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = static_cast<int>(i);
+    return v;
+}
+
 // A value read from a file, fit for an error message: printable ASCII only
 // (anything else becomes '?'), at most 64 characters.
 inline std::string printable(const std::string &v) {
@@ -488,6 +517,8 @@ private:
             if (!fin(r.x) || !fin(r.y)) return fail("non-finite detector reference");
         set_sources(sources);
         m_roiPixel = m_pixel;
+        m_detBL = det_bl;
+        m_detSize = det_px;
         return true;
     }
 
@@ -511,6 +542,8 @@ public:
         set_sources(sources);
         // built from values, the detector is taken to be the ROI
         m_detWSize = {pixelSpacing.x * static_cast<float>(roiSize.x), pixelSpacing.y * static_cast<float>(roiSize.y)};
+        m_detBL = roiBottomLeft;
+        m_detSize = roiSize;
         m_valid = true;
     }
 
@@ -530,8 +563,13 @@ public:
             if (i >= 0 && i < static_cast<int>(m_srcY.size())) m_srcY.erase(m_srcY.begin() + i);
         for (int i : indices)
             if (i >= 0 && i < static_cast<int>(m_roiBL.size())) m_roiBL.erase(m_roiBL.begin() + i);
+        for (int i : indices)
+            if (i >= 0 && i < static_cast<int>(m_detBL.size())) m_detBL.erase(m_detBL.begin() + i);
         m_size.z = 100;
-        m_pixel = {m_detWSize.x / 3048.f, m_detWSize.y / 3048.f};
+        if (m_detSize.x != 3048 || m_detSize.y != 3048) {
+            m_detSize = {3048, 3048};
+            m_pixel = {m_detWSize.x / 3048.f, m_detWSize.y / 3048.f};
+        }
         m_roiSize = {3048, 3048};
     }
     bool IsValid() const { return m_valid; }
@@ -555,8 +593,75 @@ public:
     PixelSpacing projectionsRoisPixelSpacing() const { return m_roiPixel; }
     Size3D volumeSize3D() const { return m_size; }
     VoxelSpacing volumeVoxelSpacing() const { return m_spacing; }
+    // The volume (TomoVolume): extent = count x spacing in float, centred at
+    // the origin; voxel-corner positions along each axis by repeated float
+    // addition of the spacing from the bottom-left-front corner; the grid
+    // z-major (x fastest).
+    WSize3D volumeWSize3D() const {
+        return {static_cast<float>(m_size.x) * m_spacing.x, static_cast<float>(m_size.y) * m_spacing.y,
+                static_cast<float>(m_size.z) * m_spacing.z};
+    }
     Position3D volumeBLF() const {
-        return {-0.5f * m_size.x * m_spacing.x, -0.5f * m_size.y * m_spacing.y, -0.5f * m_size.z * m_spacing.z};
+        const WSize3D w = volumeWSize3D();
+        return {-0.5f * w.x, -0.5f * w.y, -0.5f * w.z};
+    }
+    Position3D volumeTRB() const {
+        const WSize3D w = volumeWSize3D();
+        const Position3D b = volumeBLF();
+        return {b.x + w.x, b.y + w.y, b.z + w.z};
+    }
+    float volumeSize() const {
+        const WSize3D w = volumeWSize3D();
+        return w.x * w.y * w.z;
+    }
+    std::vector<float> volumeXs() const { return kvtomo_detail::axis_positions(volumeBLF().x, m_spacing.x, m_size.x); }
+    std::vector<float> volumeYs() const { return kvtomo_detail::axis_positions(volumeBLF().y, m_spacing.y, m_size.y); }
+    std::vector<float> volumeZs() const { return kvtomo_detail::axis_positions(volumeBLF().z, m_spacing.z, m_size.z); }
+    std::vector<Position3D> volumeGridPositions() const {
+        const auto xs = volumeXs(), ys = volumeYs(), zs = volumeZs();
+        std::vector<Position3D> out;
+        out.reserve(xs.size() * ys.size() * zs.size());
+        for (float z : zs)
+            for (float y : ys)
+                for (float x : xs) out.push_back({x, y, z});
+        return out;
+    }
+    std::vector<int> volumeVoxelsIndices() const {
+        return kvtomo_detail::indices(static_cast<size_t>(m_size.x) * m_size.y * m_size.z);
+    }
+
+    // The full detector and its ROI (TomoProjectionsSet): per view a
+    // bottom-left corner, a pixel count and pitch, the extent; pixel
+    // positions by repeated float addition of the pitch from the corner.
+    std::vector<Position2D> projectionsBottomLeftPositions() const { return m_detBL; }
+    Size2D projectionsSize() const { return m_detSize; }
+    WSize2D projectionsWSize() const { return m_detWSize; }
+    std::vector<std::vector<float>> projectionsXPositions() const {
+        return kvtomo_detail::view_positions(m_detBL, true, m_pixel.x, m_detSize.x);
+    }
+    std::vector<std::vector<float>> projectionsYPositions() const {
+        return kvtomo_detail::view_positions(m_detBL, false, m_pixel.y, m_detSize.y);
+    }
+    std::vector<Position2D> projectionsPositions() const {
+        return kvtomo_detail::pixel_positions(projectionsXPositions(), projectionsYPositions());
+    }
+    std::vector<int> projectionsPositionsIndices() const {
+        return kvtomo_detail::indices(m_detBL.size() * static_cast<size_t>(m_detSize.x) * m_detSize.y);
+    }
+    WSize2D projectionsRoisWSize() const {
+        return {static_cast<float>(m_roiSize.x) * m_roiPixel.x, static_cast<float>(m_roiSize.y) * m_roiPixel.y};
+    }
+    std::vector<std::vector<float>> projectionsRoisXPositions() const {
+        return kvtomo_detail::view_positions(m_roiBL, true, m_roiPixel.x, m_roiSize.x);
+    }
+    std::vector<std::vector<float>> projectionsRoisYPositions() const {
+        return kvtomo_detail::view_positions(m_roiBL, false, m_roiPixel.y, m_roiSize.y);
+    }
+    std::vector<Position2D> projectionsRoisPositions() const {
+        return kvtomo_detail::pixel_positions(projectionsRoisXPositions(), projectionsRoisYPositions());
+    }
+    std::vector<int> projectionsRoisPositionsIndices() const {
+        return kvtomo_detail::indices(m_roiBL.size() * static_cast<size_t>(m_roiSize.x) * m_roiSize.y);
     }
     WSize3D fulcrum() const { return m_fulcrum; }
 
@@ -609,6 +714,8 @@ private:
     PixelSpacing m_pixel;     // detector pitch (what the projector uses)
     PixelSpacing m_roiPixel;  // the ROI set's own pitch
     WSize2D m_detWSize;       // detector extent (mm)
+    std::vector<Position2D> m_detBL;  // per-view detector bottom-left corners
+    Size2D m_detSize;         // detector pixel counts
     WSize3D m_fulcrum;
     float m_detZ = 0.f;
     bool m_valid = false;

@@ -1,7 +1,8 @@
 // Reads a geometry file with the drop-in header's TomoGeometry(path) and
 // prints the flattened description the kernels receive, as JSON.  With
 // "adapt i j ..." after the path it first applies
-// PerformCheatingAdaptationsForDemonstration({i, j, ...}).
+// PerformCheatingAdaptationsForDemonstration({i, j, ...}); with "accessors"
+// as the last argument it prints the geometry accessors instead.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -19,6 +20,55 @@ static std::string json_escape(const std::string &v) {
     return out;
 }
 
+static void floats(const char *key, const std::vector<float> &v, bool last = false) {
+    std::printf("\"%s\": [", key);
+    for (size_t i = 0; i < v.size(); ++i) std::printf("%s%.9g", i ? ", " : "", v[i]);
+    std::printf("]%s", last ? "" : ", ");
+}
+
+static int accessors(const TomoGeometry &g) {
+    // the position lists only when small (an adapted detector has 3048^2 pixels per view)
+    std::vector<float> grid, pos, rpos;
+    const auto det_n = g.projectionsPositionsIndices().size();
+    const auto roi_n = g.projectionsRoisPositionsIndices().size();
+    for (const auto &p : g.volumeGridPositions()) grid.insert(grid.end(), {p.x, p.y, p.z});
+    if (det_n <= 100000)
+        for (const auto &p : g.projectionsPositions()) pos.insert(pos.end(), {p.x, p.y});
+    if (roi_n <= 100000)
+        for (const auto &p : g.projectionsRoisPositions()) rpos.insert(rpos.end(), {p.x, p.y});
+    const auto w = g.volumeWSize3D(), b = g.volumeBLF(), t = g.volumeTRB();
+    const auto dw = g.projectionsWSize(), rw = g.projectionsRoisWSize();
+    const auto ds = g.projectionsSize(), rs = g.projectionsRoisSize();
+    const auto dp = g.projectionsPixelSpacing(), rp = g.projectionsRoisPixelSpacing();
+    std::printf("{");
+    floats("wsize", {w.x, w.y, w.z});
+    floats("blf", {b.x, b.y, b.z});
+    floats("trb", {t.x, t.y, t.z});
+    floats("volume_size", {g.volumeSize()});
+    floats("xs", g.volumeXs());
+    floats("ys", g.volumeYs());
+    floats("zs", g.volumeZs());
+    floats("grid", grid);
+    floats("det_wsize", {dw.x, dw.y});
+    floats("det_pitch", {dp.x, dp.y});
+    floats("roi_wsize", {rw.x, rw.y});
+    floats("roi_pitch", {rp.x, rp.y});
+    std::vector<float> dbl;
+    for (const auto &p : g.projectionsBottomLeftPositions()) dbl.insert(dbl.end(), {p.x, p.y});
+    floats("det_bl", dbl);
+    floats("det_x1", g.projectionsXPositions().at(1));
+    floats("det_y1", g.projectionsYPositions().at(1));
+    floats("roi_x1", g.projectionsRoisXPositions().at(1));
+    floats("roi_y1", g.projectionsRoisYPositions().at(1));
+    floats("det_positions", pos);
+    floats("roi_positions", rpos);
+    std::printf("\"det_size\": [%d, %d], \"roi_size\": [%d, %d], \"n_voxel_indices\": %zu, "
+                "\"n_det_indices\": %zu, \"n_roi_indices\": %zu, \"last_voxel_index\": %d}\n",
+                ds.x, ds.y, rs.x, rs.y, g.volumeVoxelsIndices().size(), det_n, roi_n,
+                g.volumeVoxelsIndices().back());
+    return 0;
+}
+
 int main(int argc, char **argv) {
     if (argc < 2) return 2;
     TomoGeometry geo{std::string(argv[1])};
@@ -26,11 +76,13 @@ int main(int argc, char **argv) {
         std::printf("{\"valid\": false, \"error\": \"%s\"}\n", json_escape(geo.ErrorMessage()).c_str());
         return 0;
     }
+    const bool show_accessors = std::string(argv[argc - 1]) == "accessors";
     if (argc > 2 && std::string(argv[2]) == "adapt") {
         std::vector<int> remove;
-        for (int i = 3; i < argc; ++i) remove.push_back(std::atoi(argv[i]));
+        for (int i = 3; i < argc - (show_accessors ? 1 : 0); ++i) remove.push_back(std::atoi(argv[i]));
         geo.PerformCheatingAdaptationsForDemonstration(remove);
     }
+    if (show_accessors) return accessors(geo);
     const auto f = geo.flatten();
     const kv_geometry &g = f->g;
     std::printf("{\"valid\": true, \"n\": [%d, %d, %d], \"d\": [%.9g, %.9g, %.9g], \"views\": %d, "

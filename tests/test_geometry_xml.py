@@ -208,3 +208,61 @@ def test_demonstration_adaptations(dumper, tmp_path):
     det = np.asarray(before["det_origin"], np.float32).reshape(-1, 3)
     assert np.array_equal(np.asarray(after["src"], np.float32).reshape(-1, 3), src[keep])
     assert np.array_equal(np.asarray(after["det_origin"], np.float32).reshape(-1, 3), det[keep])
+
+
+def _positions(first, step, n):
+    out = [f32(first)]
+    for _ in range(n - 1):
+        out.append(f32(out[-1] + f32(step)))
+    return np.asarray(out, np.float32)
+
+
+def test_geometry_accessors(dumper, tmp_path):
+    """The reference's value accessors (TomoGeometry.h:34-89 over TomoVolume
+    and TomoProjectionsSet) against their construction restated in float32:
+    extents count x spacing, the volume centred, positions by repeated
+    addition of the spacing or pitch from the corner, the grid z-major, the
+    detector and ROI sets each with its own corners, size, pitch and extent;
+    then the same after the demonstration adaptation."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path, res=(3, 4, 5), roi="1 2 0 0 6 5")
+    got = json.loads(subprocess.run([dumper, path, "accessors"], check=True, capture_output=True,
+                                    text=True).stdout)
+    n, d = (5, 4, 3), (f32(0.5), f32(0.5), f32(1.0))
+    w = np.array([f32(n[k]) * d[k] for k in range(3)], np.float32)
+    blf = (f32(-0.5) * w).astype(np.float32)
+    eq = lambda a, b: np.array_equal(np.asarray(a, np.float32), np.asarray(b, np.float32))  # noqa: E731
+    assert eq(got["wsize"], w) and eq(got["blf"], blf) and eq(got["trb"], blf + w)
+    assert eq(got["volume_size"], [f32(f32(w[0] * w[1]) * w[2])])
+    axes = [_positions(blf[k], d[k], n[k]) for k in range(3)]
+    assert eq(got["xs"], axes[0]) and eq(got["ys"], axes[1]) and eq(got["zs"], axes[2])
+    grid = [(x, y, z) for z in axes[2] for y in axes[1] for x in axes[0]]
+    assert eq(np.asarray(got["grid"]).reshape(-1, 3), grid)
+    pitch = (f32(f32(40) / f32(100)), f32(f32(30) / f32(75)))
+    assert eq(got["det_wsize"], [40, 30]) and eq(got["det_pitch"], pitch) and eq(got["roi_pitch"], pitch)
+    assert got["det_size"] == [100, 75] and got["roi_size"] == [6, 4]
+    assert eq(got["roi_wsize"], [f32(6) * pitch[0], f32(4) * pitch[1]])
+    exp = expected((10.0, 20.0, 40.0), (3, 4, 5), (1.0, 0.5, 0.5), 5, (1, 2), (6, 5))
+    det_bl = [(f32(10.0 - 20.0 + 0.01 * i) - f32(10.0), f32(20.0 - 15.0) - f32(20.0)) for i in range(5)]
+    assert eq(np.asarray(got["det_bl"]).reshape(-1, 2), det_bl)
+    assert eq(got["det_x1"], _positions(det_bl[1][0], pitch[0], 100))
+    assert eq(got["det_y1"], _positions(det_bl[1][1], pitch[1], 75))
+    roi_bl = np.asarray(exp["det_origin"], np.float32).reshape(-1, 3)[:, :2]
+    assert eq(got["roi_x1"], _positions(roi_bl[1][0], pitch[0], 6))
+    assert eq(got["roi_y1"], _positions(roi_bl[1][1], pitch[1], 4))
+    rois = np.asarray(got["roi_positions"]).reshape(5, 4, 6, 2)
+    assert eq(rois[1, :, :, 0], np.tile(got["roi_x1"], (4, 1)))
+    assert eq(rois[1, :, :, 1], np.tile(np.asarray(got["roi_y1"])[:, None], (1, 6)))
+    assert np.asarray(got["det_positions"]).size == 2 * 5 * 75 * 100
+    assert got["n_voxel_indices"] == 60 and got["last_voxel_index"] == 59
+    assert got["n_det_indices"] == 5 * 75 * 100 and got["n_roi_indices"] == 5 * 4 * 6
+    # after the demonstration adaptation: 100 slices, 3048^2 detector and ROI,
+    # the detector pitch from its extent, the ROI keeping its own pitch
+    got = json.loads(subprocess.run([dumper, path, "adapt", "0", "accessors"], check=True,
+                                    capture_output=True, text=True).stdout)
+    assert eq(got["zs"], _positions(f32(-0.5) * f32(f32(100) * d[2]), d[2], 100))
+    assert got["det_size"] == [3048, 3048] and got["roi_size"] == [3048, 3048]
+    assert eq(got["det_pitch"], [f32(40) / f32(3048), f32(30) / f32(3048)]) and eq(got["roi_pitch"], pitch)
+    assert eq(got["roi_wsize"], [f32(3048) * pitch[0], f32(3048) * pitch[1]])
+    assert eq(np.asarray(got["det_bl"]).reshape(-1, 2), det_bl[1:])
+    assert got["n_roi_indices"] == 4 * 3048 * 3048
