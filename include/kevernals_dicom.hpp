@@ -231,7 +231,7 @@ inline bool read_file(const std::string &path, Image &img, std::string &err) {
 class DICOMReader {
 public:
     DICOMReader() = delete;
-    explicit DICOMReader(TomoGeometry *p_tomoGeometry) : m_geo(p_tomoGeometry) {}
+    DICOMReader(TomoGeometry *p_tomoGeometry) : m_geo(p_tomoGeometry) {}
 
     // One projection image, cropped to the geometry's detector ROI.
     Result<ImageDataPtr> Read(const std::string &p_dicomFilePath) const {

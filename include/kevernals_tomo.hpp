@@ -841,7 +841,7 @@ inline bool WriteTIFF(const std::string &path, const ImageDataPtr &img) {
 
 class Projector {
 public:
-    explicit Projector(TomoGeometry *p_tomoGeometry, kv_family family = KV_FAMILY_RC)
+    Projector(TomoGeometry *p_tomoGeometry, kv_family family = KV_FAMILY_RC)
         : m_tomoGeometry(p_tomoGeometry), m_family(family) {}
 
     // Projector::PerformProjection, Projector.cu:873-1036.  Returns nullptr on failure.
