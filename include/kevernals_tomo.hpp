@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <iostream>
 #include <sstream>
 #include <memory>
 #include <optional>
@@ -996,12 +997,17 @@ inline Result<ImageDataPtr> FilteredBackProjection(TomoGeometry *p_tomoGeometry,
 }
 
 // recons::ShiftAndAdd, Reconstructors.h:263-379: one detector-sized slice per
-// volume slice.
+// volume slice.  Verbose mode (an output directory given) prints the fulcrum
+// height and the source-to-image distance, as the reference does; it writes
+// no files.
 inline Result<ImageDataPtr> ShiftAndAdd(TomoGeometry *p_tomoGeometry, ImageDataPtr p_projectionImages,
                                         std::optional<std::string> p_outputDirectoryPath = std::nullopt,
                                         kv_family family = KV_FAMILY_RC) {
-    (void)p_outputDirectoryPath;
     if (p_tomoGeometry == nullptr || p_projectionImages == nullptr) return ReconstructorsErrorCode::ShiftAndAdd;
+    if (p_outputDirectoryPath.has_value()) {
+        std::cout << "zF = " << std::to_string(p_tomoGeometry->fulcrum().z) << std::endl;
+        std::cout << "sid = " << std::to_string(p_tomoGeometry->sid()) << std::endl;
+    }
     Projector projector{p_tomoGeometry, family};
     kv_plan *plan = projector.plan();
     if (plan == nullptr || p_projectionImages->size() != kv_plan_proj_elems(plan))
