@@ -33,6 +33,7 @@
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <limits>
 #include <sstream>
 #include <memory>
 #include <optional>
@@ -931,14 +932,30 @@ inline Result<ImageDataPtr> iterate(bool mlem, TomoGeometry *g, ImageDataPtr pro
         if (run(plan, proj->data(), x->data(), iters, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
         return x;
     }
-    // verbose mode: the initial volume and every iterate as multi-page TIFFs,
-    // named as the reference names them (Reconstructors.h:47-53, 125-131); the
-    // per-iteration projection dumps are not written (the fused kernels keep
-    // them on the device)
-    WriteTIFF(outDir.value() + "initialVolume.tiff", x);
+    // verbose mode, with the reference's files (Reconstructors.h:47-131,
+    // 164-248) as multi-page TIFFs: the initial volume; per iteration the
+    // projection A x, the corrected projection -- relax (p - A x) for ART,
+    // relax p / A x where A x is not zero (AlmostEqualRelative, float
+    // epsilon) and A x elsewhere for MLEM -- and the new iterate.  The fused
+    // kernels keep the projections on the device, so in this mode each
+    // iteration runs one extra forward projection to the host for the dumps.
+    const std::string dir = outDir.value();
+    WriteTIFF(dir + "initialVolume.tiff", x);
     for (int it = 0; it < iters; ++it) {
+        const std::string step = std::to_string(it) + ".tiff";
+        ImageDataPtr q = projector.PerformProjection(x);
+        if (q == nullptr) return code;
+        WriteTIFF(dir + "currentProjectionStep" + step, q);
+        const float *p = proj->data();
+        float *c = q->data();
+        const float eps = std::numeric_limits<float>::epsilon();
+        for (size_t i = 0; i < q->size(); ++i) {
+            if (!mlem) c[i] = relax * (p[i] - c[i]);
+            else if (!(std::fabs(c[i]) <= eps * std::fabs(c[i]))) c[i] = relax * (p[i] / c[i]);
+        }
+        WriteTIFF(dir + "currentCorrectedProjectionStep" + step, q);
         if (run(plan, proj->data(), x->data(), 1, relax, KV_MEM_HOST, nullptr, nullptr) != KV_OK) return code;
-        WriteTIFF(outDir.value() + "reconstructionstep" + std::to_string(it) + ".tiff", x);
+        WriteTIFF(dir + "reconstructionstep" + step, x);
     }
     return x;
 }

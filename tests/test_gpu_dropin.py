@@ -60,11 +60,16 @@ def test_cpp_dropin(tmp_path):
     fbp = load("exact_fbp.raw", g.volume_shape).astype(np.float64)
     ref = O.exact_fbp(g, load("exact_fwd.raw", g.proj_shape), 16)
     assert np.linalg.norm(fbp - ref) <= 1e-5 * np.linalg.norm(ref)
-    # verbose MLEM: TIFF pages (rows top first) equal the iterates
+    # verbose MLEM: TIFF pages (rows top first) equal the iterates, the
+    # projections A x and the corrected projections 0.5 p / A x (A x where 0)
     from test_output_tools import read_tiff
+    tif = lambda name: read_tiff(str(tmp_path / name))[:, ::-1, :]  # noqa: E731
     x = ones
     for it in range(2):
+        q = O.rc_forward(g, x)
+        assert np.array_equal(tif(f"verbose_currentProjectionStep{it}.tiff"), q)
+        corrected = np.where(q != 0, np.float32(0.5) * (proj / np.where(q != 0, q, np.float32(1))), q)
+        assert np.array_equal(tif(f"verbose_currentCorrectedProjectionStep{it}.tiff"), corrected.astype(np.float32))
         x = O.rc_mlem(g, proj, x, 1, 0.5)
-        got = read_tiff(str(tmp_path / f"verbose_reconstructionstep{it}.tiff"))[:, ::-1, :]
-        assert np.array_equal(got, x)
+        assert np.array_equal(tif(f"verbose_reconstructionstep{it}.tiff"), x)
     assert np.array_equal(read_tiff(str(tmp_path / "verbose_initialVolume.tiff"))[:, ::-1, :], ones)
