@@ -197,6 +197,7 @@ public:
     void GetSpacing(double out[3]) const {
         for (int i = 0; i < 3; ++i) out[i] = m_spacing[i];
     }
+    const double *GetSpacing() const { return m_spacing; }
     void SetOrigin(double x, double y, double z) {
         m_origin[0] = x;
         m_origin[1] = y;
@@ -205,9 +206,39 @@ public:
     void GetOrigin(double out[3]) const {
         for (int i = 0; i < 3; ++i) out[i] = m_origin[i];
     }
+    const double *GetOrigin() const { return m_origin; }
+    // whole extent [0, nx-1, 0, ny-1, 0, nz-1], as vtkImageData::GetExtent
+    void GetExtent(int out[6]) const {
+        for (int i = 0; i < 3; ++i) {
+            out[2 * i] = 0;
+            out[2 * i + 1] = m_dims[i] - 1;
+        }
+    }
+    long long GetNumberOfPoints() const { return static_cast<long long>(size()); }
+    // dimensions, spacing, origin and a copy of the scalars
+    void DeepCopy(const ImageData *src) {
+        if (src == nullptr || src == this) return;
+        *this = *src;
+    }
+    void DeepCopy(const std::shared_ptr<ImageData> &src) { DeepCopy(src.get()); }
     // VTK_FLOAT with one component is the only scalar type used on this path.
     void AllocateScalars(int = 0, int = 1) { m_data.assign(size(), 0.f); }
     void *GetScalarPointer() { return m_data.data(); }
+    // the scalar at voxel (x, y, z), x fastest; nullptr outside the image
+    void *GetScalarPointer(int x, int y, int z) {
+        if (x < 0 || y < 0 || z < 0 || x >= m_dims[0] || y >= m_dims[1] || z >= m_dims[2] || m_data.empty())
+            return nullptr;
+        return m_data.data() + (static_cast<size_t>(z) * m_dims[1] + y) * m_dims[0] + x;
+    }
+    // one component (c = 0) per voxel
+    float GetScalarComponentAsFloat(int x, int y, int z, int c) {
+        const float *p = static_cast<const float *>(GetScalarPointer(x, y, z));
+        return (p != nullptr && c == 0) ? *p : 0.f;
+    }
+    void SetScalarComponentFromFloat(int x, int y, int z, int c, float v) {
+        float *p = static_cast<float *>(GetScalarPointer(x, y, z));
+        if (p != nullptr && c == 0) *p = v;
+    }
     const float *data() const { return m_data.data(); }
     float *data() { return m_data.data(); }
     size_t size() const { return (size_t)m_dims[0] * m_dims[1] * m_dims[2]; }

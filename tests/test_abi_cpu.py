@@ -123,6 +123,21 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
                    '    os << g;\n'
                    '    for (const char *h : {"volume ", "projections: ", "projections Rois: ", "table: "})\n'
                    '        if (os.str().find(h) == std::string::npos) return 4;\n'
+                   '    auto im = ImageData::New();\n'
+                   '    im->SetDimensions(3, 2, 2);\n'
+                   '    im->SetSpacing(0.5, 0.25, 2.0);\n'
+                   '    im->AllocateScalars();\n'
+                   '    im->SetScalarComponentFromFloat(2, 1, 1, 0, 7.f);\n'
+                   '    if (im->data()[(1 * 2 + 1) * 3 + 2] != 7.f || im->GetScalarComponentAsFloat(2, 1, 1, 0) != 7.f)\n'
+                   '        return 5;\n'
+                   '    if (im->GetScalarPointer(3, 0, 0) != nullptr || im->GetNumberOfPoints() != 12) return 6;\n'
+                   '    int ext[6];\n'
+                   '    im->GetExtent(ext);\n'
+                   '    if (ext[1] != 2 || ext[3] != 1 || ext[5] != 1 || im->GetSpacing()[2] != 2.0) return 7;\n'
+                   '    auto cp = ImageData::New();\n'
+                   '    cp->DeepCopy(im);\n'
+                   '    im->data()[0] = 1.f;\n'
+                   '    if (cp->data()[0] != 0.f || cp->data()[11] != 7.f || cp->GetSpacing()[0] != 0.5) return 8;\n'
                    '    return 0;\n}\n')
     example = os.path.join(root, "tests", "cpp", "reconstruct_example.cpp")
     for f in (str(src), os.path.join(root, "tests", "cpp", "test_dropin.cpp"), example):
