@@ -236,3 +236,57 @@ def test_reference_gpu_guard_agrees_with_reference_hit_test():
                     assert lib.kvo_rc_ray_hits(cg, p, u, v)
     assert not ref_gpu.all_rays_cross_volume(config_small())
     assert not ref_gpu.all_rays_cross_volume(linear_sweep(64, 48, 16, 0.5, 0.5, 1.0, 5, 80, 60, 0.4, 0.4, 20.0))
+
+
+def test_oracle_runs_clean_under_sanitizers(tmp_path):
+    """The C oracle built with AddressSanitizer and UBSan, driven through its
+    Python wrapper in a child process on geometries with missed rays, odd
+    sizes and oblique sweeps: no sanitizer report, same results as the
+    normal build."""
+    import shutil
+    import subprocess
+    import sys
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    runtimes = [subprocess.run(["gcc", f"-print-file-name={n}"], capture_output=True, text=True).stdout.strip()
+                for n in ("libasan.so", "libubsan.so")]
+    if not all(os.path.isabs(r) and os.path.exists(r) for r in runtimes):
+        pytest.skip("sanitizer runtimes not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = str(tmp_path / "liboracle_asan.so")
+    subprocess.run(["gcc", "-std=c11", "-O1", "-g", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                    "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                    os.path.join(root, "oracle", "kvtomo_oracle.c"), "-o", so, "-lm"], check=True)
+    script = f"""
+import sys
+sys.path.insert(0, {root!r})
+import numpy as np
+from oracle import build as b
+b.build_oracle = lambda *a, **k: {so!r}
+from oracle import oracle as O
+from kevernals_gb300 import phantom as ph
+from kevernals_gb300.geometry import linear_sweep
+out = []
+for g in (linear_sweep(33, 29, 7, 0.7, 0.45, 1.3, 4, 37, 41, 0.55, 0.35, 22.0),
+          linear_sweep(16, 16, 4, 0.5, 0.5, 1.0, 3, 64, 48, 0.4, 0.4, 10.0)):
+    vol = O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 5, 3))
+    p = O.rc_forward(g, vol)
+    e = O.exact_forward(g, vol.astype(np.float64))
+    out += [p, O.rc_back(g, p), O.rc_mlem(g, p, np.ones(g.volume_shape, np.float32), 2, 0.5),
+            O.rc_art(g, p, np.ones(g.volume_shape, np.float32), 2, 0.5), e, O.exact_back(g, e),
+            O.exact_mlem(g, e, np.ones(g.volume_shape), 2), O.exact_fbp(g, e, 8), O.saa_shifts(g, 0)]
+np.savez({str(tmp_path / "asan.npz")!r}, *out)
+"""
+    env = dict(os.environ, LD_PRELOAD=":".join(runtimes), ASAN_OPTIONS="detect_leaks=0:halt_on_error=1",
+               OMP_NUM_THREADS="2")
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and "ERROR" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-3000:]
+    got = np.load(tmp_path / "asan.npz")
+    i = 0
+    for g in (linear_sweep(33, 29, 7, 0.7, 0.45, 1.3, 4, 37, 41, 0.55, 0.35, 22.0),
+              linear_sweep(16, 16, 4, 0.5, 0.5, 1.0, 3, 64, 48, 0.4, 0.4, 10.0)):
+        vol = O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 5, 3))
+        p = O.rc_forward(g, vol)
+        assert np.array_equal(got[f"arr_{i}"], p)
+        assert np.array_equal(got[f"arr_{i + 1}"], O.rc_back(g, p))
+        i += 9
