@@ -159,3 +159,63 @@ def test_cpp_dropin_compiles_and_links(lib, tmp_path):
             write_xml(str(tmp_path / "geo.xml"))
             r = run(str(tmp_path / "geo.xml"), str(tmp_path / "no_series"), str(tmp_path) + "/")
             assert r.returncode == 1 and "does not exist" in r.stdout and "projections Rois:" in r.stdout
+
+
+def test_host_entry_points_run_clean_under_sanitizers(lib, tmp_path):
+    """kv_api.cu (the C ABI's host logic) rebuilt with AddressSanitizer and
+    UBSan and linked with the normal kernel objects, then driven in a child
+    process through the host-only entry points: the shift-and-add rule on
+    ordinary, oblique and hostile geometries (huge shifts are limited, NaN
+    refused), status strings and the no-device path.  No sanitizer report."""
+    import shutil
+    import subprocess
+    import sys
+    runtimes = [subprocess.run(["gcc", f"-print-file-name={n}"], capture_output=True, text=True).stdout.strip()
+                for n in ("libasan.so", "libubsan.so")]
+    if shutil.which("gcc") is None or not all(os.path.isabs(r) and os.path.exists(r) for r in runtimes):
+        pytest.skip("sanitizer runtimes not available")
+    from kevernals_gb300 import build as kb
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    csrc = os.path.join(root, "kevernals_gb300", "csrc")
+    api = str(tmp_path / "kv_api.o")
+    subprocess.run([kb.nvcc(), "-std=c++17", "-O1", "-g", *kb.ARCH, "-Xcompiler",
+                    "-fPIC,-fsanitize=address,-fsanitize=undefined,-fno-omit-frame-pointer",
+                    "-I", os.path.join(root, "include"), "-I", csrc, "-c", os.path.join(csrc, "kv_api.cu"),
+                    "-o", api], check=True, capture_output=True)
+    objs = [os.path.join(kb.BUILD, f"{s}.o") for s in ("kv_exact", "kv_rc", "kv_misc", "kv_unet")]
+    so = str(tmp_path / "libkvtomo_asan.so")
+    subprocess.run([kb.nvcc(), "-shared", *kb.ARCH, "-o", so, api, *objs, "-lcudart", "-Xcompiler",
+                    "-fsanitize=address,-fsanitize=undefined"], check=True, capture_output=True)
+    script = f"""
+import dataclasses, sys
+sys.path.insert(0, {root!r})
+import ctypes as C
+import numpy as np
+from kevernals_gb300 import _lib
+_lib.LIB_PATH = {so!r}
+from kevernals_gb300 import engine
+from kevernals_gb300.geometry import config_chest, config_small, linear_sweep
+L = _lib.lib()
+assert L.kv_status_string(0) == b"ok"
+h = C.c_void_p()
+assert L.kv_ctx_create(0, C.byref(h)) == 8 and L.kv_ctx_destroy(None) == 1
+for g in (config_small(), config_chest(), linear_sweep(32, 32, 17, 0.4, 0.4, 2.5, 9, 64, 4, 0.3, 0.3, 25.0),
+          linear_sweep(8, 8, 2, 0.5, 0.5, 1.0, 3, 8, 8, 0.5, 0.5, 89.0)):
+    for fam in ("rc", "exact"):
+        engine.shift_and_add_shifts(g, fam)
+g = linear_sweep(8, 8, 4, 0.5, 0.5, 1.0, 3, 8, 8, 0.5, 0.5, 10.0)
+src = g.src.copy()
+src[:, 1] = np.float32(3e38)
+assert np.abs(engine.shift_and_add_shifts(dataclasses.replace(g, src=src), "rc")).max() == 1 << 30
+for bad in (dataclasses.replace(g, fulcrum_z=float("nan")), dataclasses.replace(g, dz=float("inf"))):
+    for fam in ("rc", "exact"):
+        try:
+            engine.shift_and_add_shifts(bad, fam)
+            raise SystemExit("accepted a non-finite geometry")
+        except _lib.KvError:
+            pass
+"""
+    env = dict(os.environ, LD_PRELOAD=":".join(runtimes), ASAN_OPTIONS="detect_leaks=0:halt_on_error=1",
+               UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and "ERROR" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-3000:]
