@@ -422,7 +422,7 @@ public:
     // ROI's bottom-left position of view i is the detector corner plus the
     // pixel pitch added pixel by pixel in float (TomoProjectionsSet.cpp:
     // 172-190, 152-155), the pitch being extent / count (PixelSpacing.cpp).
-    explicit TomoGeometry(const std::string &xmlPath) { m_valid = read_xml(xmlPath); }
+    explicit TomoGeometry(const std::string &xmlPath) : m_filePath(xmlPath) { m_valid = read_xml(xmlPath); }
 
 private:
     bool read_xml(const std::string &xmlPath) {
@@ -552,6 +552,7 @@ private:
         m_roiPixel = m_pixel;
         m_detBL = det_bl;
         m_detSize = det_px;
+        m_blf = centred_corner();
         return true;
     }
 
@@ -577,6 +578,7 @@ public:
         m_detWSize = {pixelSpacing.x * static_cast<float>(roiSize.x), pixelSpacing.y * static_cast<float>(roiSize.y)};
         m_detBL = roiBottomLeft;
         m_detSize = roiSize;
+        m_blf = centred_corner();
         m_valid = true;
     }
 
@@ -588,7 +590,10 @@ public:
     // the volume 100 slices of the same spacing, and resamples the detector
     // and its ROI to 3048 x 3048 pixels: the detector pitch, the one the
     // projector uses, becomes the detector's width / 3048, while the ROI
-    // corners and the ROI's own pitch keep their values.
+    // corners and the ROI's own pitch keep their values.  As in the
+    // reference the volume keeps its bottom-left-front corner, so that after
+    // the change of slice count it is no longer centred in z (its positions
+    // say so; the projector, in both, treats every volume as centred).
     void PerformCheatingAdaptationsForDemonstration(const std::vector<int> &p_dataIndicesToRemove) {
         auto indices = p_dataIndicesToRemove;
         std::sort(indices.begin(), indices.end(), std::greater<int>());
@@ -626,18 +631,16 @@ public:
     PixelSpacing projectionsRoisPixelSpacing() const { return m_roiPixel; }
     Size3D volumeSize3D() const { return m_size; }
     VoxelSpacing volumeVoxelSpacing() const { return m_spacing; }
-    // The volume (TomoVolume): extent = count x spacing in float, centred at
-    // the origin; voxel-corner positions along each axis by repeated float
-    // addition of the spacing from the bottom-left-front corner; the grid
-    // z-major (x fastest).
+    // The volume (TomoVolume): extent = count x spacing in float, the
+    // bottom-left-front corner at minus half the extent when read or built
+    // (a centred volume); voxel-corner positions along each axis by repeated
+    // float addition of the spacing from that corner; the grid z-major (x
+    // fastest).
     WSize3D volumeWSize3D() const {
         return {static_cast<float>(m_size.x) * m_spacing.x, static_cast<float>(m_size.y) * m_spacing.y,
                 static_cast<float>(m_size.z) * m_spacing.z};
     }
-    Position3D volumeBLF() const {
-        const WSize3D w = volumeWSize3D();
-        return {-0.5f * w.x, -0.5f * w.y, -0.5f * w.z};
-    }
+    Position3D volumeBLF() const { return m_blf; }
     Position3D volumeTRB() const {
         const WSize3D w = volumeWSize3D();
         const Position3D b = volumeBLF();
@@ -697,6 +700,9 @@ public:
         return kvtomo_detail::indices(m_roiBL.size() * static_cast<size_t>(m_roiSize.x) * m_roiSize.y);
     }
     WSize3D fulcrum() const { return m_fulcrum; }
+    WSize3D rotationCenter() const { return m_fulcrum; }
+    // the geometry file read ("" when built from values)
+    std::string filePath() const { return m_filePath; }
 
     // Flattened description the kernels consume (Projector.cu:917-940):
     // sources (common x, y_i, common z), ROI origins (x_i, y_i, common z).
@@ -724,6 +730,11 @@ public:
     }
 
 private:
+    Position3D centred_corner() const {
+        const WSize3D w = volumeWSize3D();
+        return {-0.5f * w.x, -0.5f * w.y, -0.5f * w.z};
+    }
+
     // common source x and z: float sums over the views (TomoTable.cpp:4-19)
     void set_sources(const std::vector<Position3D> &sources) {
         float sx = 0.f, sz = 0.f;
@@ -748,11 +759,13 @@ private:
     PixelSpacing m_roiPixel;  // the ROI set's own pitch
     WSize2D m_detWSize;       // detector extent (mm)
     std::vector<Position2D> m_detBL;  // per-view detector bottom-left corners
+    Position3D m_blf;         // the volume's bottom-left-front corner
     Size2D m_detSize;         // detector pixel counts
     WSize3D m_fulcrum;
     float m_detZ = 0.f;
     bool m_valid = false;
     std::string m_error;
+    std::string m_filePath;
 };
 
 // A readable summary under the reference printer's headings

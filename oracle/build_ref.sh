@@ -6,9 +6,18 @@
 #   oracle/_ref/ref_kernels.cubin    compiled for sm_103a as the reference
 #                                    ships them (nvcc defaults, FMA contraction on)
 #   oracle/_ref/ref_kernels_nofma.cubin  the same with -fmad=false
-# (the cubins only when nvcc is on PATH).
+# (the cubins only when nvcc is on PATH), and from the reference's geometry
+# module (source/modules/geometry/*.cpp with the vendored
+# source/commons/tinyXML/tinyxml2.cpp, compiled where they lie):
+#   oracle/_ref/ref_geometry         the reference's XML geometry reader behind
+#                                    ref_geometry_driver.cpp; two headers that
+#                                    gcc rejects are replaced by the stand-ins
+#                                    in ref_geometry_shim/ (first on the
+#                                    include path); TomoGeometryErrorCode.cpp is
+#                                    left out (unused by the reader)
 # TEST INFRASTRUCTURE: checkers for the RC restatement in kvtomo_oracle.c and
-# for the engine's RC kernels, and the "reference GPU" timing line.
+# for the engine's RC kernels, the "reference GPU" timing line, and the
+# checker for the drop-in's XML geometry reader.
 #
 # Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
 # The kernel lines are extracted into oracle/_ref/ only for the compile and
@@ -39,3 +48,12 @@ if command -v nvcc > /dev/null; then
     rm -f "$out/ref_kernels_gpu.inc"
     echo "build_ref: built $out/ref_kernels.cubin, $out/ref_kernels_nofma.cubin"
 fi
+geo=()
+for f in "$ref"/source/modules/geometry/*.cpp; do
+    case "$f" in *_test.cpp|*/TomoGeometryErrorCode.cpp) continue ;; esac
+    geo+=("$f")
+done
+g++ -std=c++17 -O1 -w -fpermissive -I "$here/ref_geometry_shim" -I "$ref/source" \
+    "$here/ref_geometry_driver.cpp" "${geo[@]}" "$ref/source/commons/tinyXML/tinyxml2.cpp" \
+    -o "$out/ref_geometry"
+echo "build_ref: built $out/ref_geometry"

@@ -256,13 +256,82 @@ def test_geometry_accessors(dumper, tmp_path):
     assert np.asarray(got["det_positions"]).size == 2 * 5 * 75 * 100
     assert got["n_voxel_indices"] == 60 and got["last_voxel_index"] == 59
     assert got["n_det_indices"] == 5 * 75 * 100 and got["n_roi_indices"] == 5 * 4 * 6
-    # after the demonstration adaptation: 100 slices, 3048^2 detector and ROI,
-    # the detector pitch from its extent, the ROI keeping its own pitch
+    # after the demonstration adaptation: 100 slices from the same corner (the
+    # volume no longer centred in z, as in the reference), 3048^2 detector and
+    # ROI, the detector pitch from its extent, the ROI keeping its own pitch
     got = json.loads(subprocess.run([dumper, path, "adapt", "0", "accessors"], check=True,
                                     capture_output=True, text=True).stdout)
-    assert eq(got["zs"], _positions(f32(-0.5) * f32(f32(100) * d[2]), d[2], 100))
+    assert eq(got["blf"], blf) and eq(got["zs"], _positions(blf[2], d[2], 100))
     assert got["det_size"] == [3048, 3048] and got["roi_size"] == [3048, 3048]
     assert eq(got["det_pitch"], [f32(40) / f32(3048), f32(30) / f32(3048)]) and eq(got["roi_pitch"], pitch)
     assert eq(got["roi_wsize"], [f32(3048) * pitch[0], f32(3048) * pitch[1]])
     assert eq(np.asarray(got["det_bl"]).reshape(-1, 2), det_bl[1:])
     assert got["n_roi_indices"] == 4 * 3048 * 3048
+
+
+# ---- against the reference's own reader ------------------------------------
+
+@pytest.fixture(scope="module")
+def ref_reader():
+    """The reference's XML reader (its geometry module and tinyxml2, compiled
+    from the reference tree by oracle/build_ref.sh); absent without the tree."""
+    from oracle import build as ob
+    ob.build_ref()
+    if not os.path.exists(ob.REF_GEOMETRY):
+        pytest.skip("reference geometry reader not built (needs the reference tree)")
+    return ob.REF_GEOMETRY
+
+
+def _ref_read(ref_reader, *args):
+    out = subprocess.run([ref_reader, *args], check=True, capture_output=True, text=True).stdout
+    return json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+
+
+VARIANTS = [
+    {},
+    {"centre": (-3.5, 7.25, 12.0), "res": (7, 33, 21), "scale": (2.5, 0.4, 0.3), "views": 9,
+     "roi": "0 0 0 0 99 74"},
+    {"roi": "-5 3 0 0 150 90"},                     # corners clamped to the detector
+    {"views": 1, "roi": "40 30 0 0 40 30"},          # one view, a one-pixel ROI
+    {"centre": (0.125, -250.0, 600.0), "res": (64, 16, 8), "scale": (0.7, 1.1, 0.9), "views": 4},
+]
+
+
+@pytest.mark.parametrize("i", range(len(VARIANTS)))
+def test_xml_reader_matches_reference_reader(dumper, ref_reader, tmp_path, i):
+    """The drop-in's reader and the reference's own reader on the same files:
+    what the projector receives is equal bit for bit."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path, **VARIANTS[i])
+    ours, ref = read(dumper, path), _ref_read(ref_reader, path)
+    assert ours["valid"] and ref["valid"], (ours, ref)
+    for k in ("n", "views", "det"):
+        assert ours[k] == ref[k], k
+    for k in ("d", "pitch", "src", "det_origin", "fulcrum_z"):
+        assert np.array_equal(np.asarray(ours[k], np.float32), np.asarray(ref[k], np.float32)), k
+
+
+@pytest.mark.parametrize("args", [("accessors",), ("adapt", "3", "0", "9", "3", "accessors")])
+def test_xml_accessors_match_reference_reader(dumper, ref_reader, tmp_path, args):
+    """Every value accessor, before and after the demonstration adaptation,
+    equal to the reference reader's."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path, res=(3, 4, 5), roi="1 2 0 0 6 5")
+    ours = json.loads(subprocess.run([dumper, path, *args], check=True, capture_output=True, text=True).stdout)
+    ref = _ref_read(ref_reader, path, *args)
+    assert set(ours) == set(ref)
+    for k, v in ref.items():
+        if isinstance(v, list) and v and isinstance(v[0], float) or k.endswith(("wsize", "pitch", "size")):
+            assert np.array_equal(np.asarray(ours[k], np.float32), np.asarray(v, np.float32)), k
+        else:
+            assert ours[k] == v, k
+
+
+def test_xml_invalid_files_match_reference_reader(dumper, ref_reader, tmp_path):
+    """Files both readers refuse: a missing section, ROIs that differ between
+    views, a truncated file."""
+    path = str(tmp_path / "bad.xml")
+    for kw in ({"drop": "Grid"}, {"drop": "Rotation"},
+               {"rois": ["10 20 0 0 89 79"] * 2 + ["11 20 0 0 89 79"] + ["10 20 0 0 89 79"] * 2}):
+        write_xml(path, **kw)
+        assert not read(dumper, path)["valid"] and not _ref_read(ref_reader, path)["valid"], kw
