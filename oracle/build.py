@@ -8,6 +8,8 @@ _ref/libkvref.so  the reference's own kernels, compiled from the reference
                GPU cubins _ref/ref_kernels*.cubin, see ref_gpu.py).
 _ref/ref_geometry  the reference's XML geometry reader (its geometry module
                and tinyxml2) behind ref_geometry_driver.cpp, the same way.
+_ref/ref_histogram  the reference's histogram tools behind
+               ref_histogram_driver.cpp, against ref_vtk_stub/.
 """
 import os
 import subprocess
@@ -16,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libkvref.so")
 REF_GEOMETRY = os.path.join(HERE, "_ref", "ref_geometry")
+REF_HISTOGRAM = os.path.join(HERE, "_ref", "ref_histogram")
 REFERENCE_ROOT = "/root/reference"
 
 
@@ -35,8 +38,7 @@ def build_ref(force=False):
     if not os.path.isdir(REFERENCE_ROOT):
         return None
     cubins = [os.path.join(HERE, "_ref", f) for f in ("ref_kernels.cubin", "ref_kernels_nofma.cubin")]
-    if (not force and os.path.exists(REF_SO) and os.path.exists(REF_GEOMETRY)
-            and all(os.path.exists(c) for c in cubins)):
+    if (not force and all(os.path.exists(f) for f in (REF_SO, REF_GEOMETRY, REF_HISTOGRAM, *cubins))):
         return REF_SO
     subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
     return REF_SO if os.path.exists(REF_SO) else None

@@ -15,6 +15,11 @@
 #                                    in ref_geometry_shim/ (first on the
 #                                    include path); TomoGeometryErrorCode.cpp is
 #                                    left out (unused by the reader)
+#   oracle/_ref/ref_histogram        the reference's histogram tools
+#                                    (source/commons/HistogramMatchingTools.h)
+#                                    behind ref_histogram_driver.cpp, against
+#                                    the VTK stand-ins in ref_vtk_stub/ (the
+#                                    header needs only an unsigned-short image)
 # TEST INFRASTRUCTURE: checkers for the RC restatement in kvtomo_oracle.c and
 # for the engine's RC kernels, the "reference GPU" timing line, and the
 # checker for the drop-in's XML geometry reader.
@@ -57,3 +62,6 @@ g++ -std=c++17 -O1 -w -fpermissive -I "$here/ref_geometry_shim" -I "$ref/source"
     "$here/ref_geometry_driver.cpp" "${geo[@]}" "$ref/source/commons/tinyXML/tinyxml2.cpp" \
     -o "$out/ref_geometry"
 echo "build_ref: built $out/ref_geometry"
+g++ -std=c++17 -O1 -w -fpermissive -include climits -I "$here/ref_vtk_stub" -I "$ref/source" \
+    "$here/ref_histogram_driver.cpp" -o "$out/ref_histogram"
+echo "build_ref: built $out/ref_histogram"
