@@ -10,6 +10,8 @@ _ref/ref_geometry  the reference's XML geometry reader (its geometry module
                and tinyxml2) behind ref_geometry_driver.cpp, the same way.
 _ref/ref_histogram  the reference's histogram tools behind
                ref_histogram_driver.cpp, against ref_vtk_stub/.
+_ref/ref_drivers  the reference's ART / MLEM drivers (Reconstructors.h) on
+               the host build of its kernels, behind ref_drivers_main.cpp.
 """
 import os
 import subprocess
@@ -19,6 +21,7 @@ ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libkvref.so")
 REF_GEOMETRY = os.path.join(HERE, "_ref", "ref_geometry")
 REF_HISTOGRAM = os.path.join(HERE, "_ref", "ref_histogram")
+REF_DRIVERS = os.path.join(HERE, "_ref", "ref_drivers")
 REFERENCE_ROOT = "/root/reference"
 
 
@@ -38,7 +41,7 @@ def build_ref(force=False):
     if not os.path.isdir(REFERENCE_ROOT):
         return None
     cubins = [os.path.join(HERE, "_ref", f) for f in ("ref_kernels.cubin", "ref_kernels_nofma.cubin")]
-    if (not force and all(os.path.exists(f) for f in (REF_SO, REF_GEOMETRY, REF_HISTOGRAM, *cubins))):
+    if (not force and all(os.path.exists(f) for f in (REF_SO, REF_GEOMETRY, REF_HISTOGRAM, REF_DRIVERS, *cubins))):
         return REF_SO
     subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True)
     return REF_SO if os.path.exists(REF_SO) else None

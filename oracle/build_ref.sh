@@ -15,6 +15,14 @@
 #                                    in ref_geometry_shim/ (first on the
 #                                    include path); TomoGeometryErrorCode.cpp is
 #                                    left out (unused by the reader)
+#   oracle/_ref/ref_drivers          the reference's ART and MLEM drivers
+#                                    (Reconstructors.h) with PhantomMaker's
+#                                    uniform start, behind ref_drivers_main.cpp,
+#                                    on the host build of the reference kernels
+#                                    (libkvref.so) through the Projector
+#                                    stand-in in ref_driver_shim/ and the VTK
+#                                    stand-ins in ref_vtk_stub/ (those of the
+#                                    shift-and-add filters abort if called)
 #   oracle/_ref/ref_histogram        the reference's histogram tools
 #                                    (source/commons/HistogramMatchingTools.h)
 #                                    behind ref_histogram_driver.cpp, against
@@ -53,15 +61,33 @@ if command -v nvcc > /dev/null; then
     rm -f "$out/ref_kernels_gpu.inc"
     echo "build_ref: built $out/ref_kernels.cubin, $out/ref_kernels_nofma.cubin"
 fi
+# the reference's geometry module, tinyxml2, PhantomMaker and the error
+# categories, compiled once (in parallel) for the two checkers below
+flags=(-std=c++17 -O1 -w -fpermissive -include cstring -include climits -I "$here/ref_driver_shim"
+       -I "$here/ref_geometry_shim" -I "$here/ref_vtk_stub" -I "$ref/source")
+obj="$out/obj"
+mkdir -p "$obj"
 geo=()
-for f in "$ref"/source/modules/geometry/*.cpp; do
+for f in "$ref"/source/modules/geometry/*.cpp "$ref/source/commons/tinyXML/tinyxml2.cpp"; do
     case "$f" in *_test.cpp|*/TomoGeometryErrorCode.cpp) continue ;; esac
     geo+=("$f")
 done
-g++ -std=c++17 -O1 -w -fpermissive -I "$here/ref_geometry_shim" -I "$ref/source" \
-    "$here/ref_geometry_driver.cpp" "${geo[@]}" "$ref/source/commons/tinyXML/tinyxml2.cpp" \
-    -o "$out/ref_geometry"
+extra=("$ref/source/modules/dataHandling/PhantomMaker.cpp" "$ref/source/commons/TomoErrorCondition.cpp"
+       "$ref/source/modules/reconstruction/ReconstructorsErrorCode.cpp")
+pids=()
+for f in "${geo[@]}" "${extra[@]}"; do
+    g++ "${flags[@]}" -c "$f" -o "$obj/$(basename "$f" .cpp).o" &
+    pids+=($!)
+done
+for p in "${pids[@]}"; do wait "$p"; done
+geo_obj=()
+for f in "${geo[@]}"; do geo_obj+=("$obj/$(basename "$f" .cpp).o"); done
+g++ "${flags[@]}" "$here/ref_geometry_driver.cpp" "${geo_obj[@]}" -o "$out/ref_geometry"
 echo "build_ref: built $out/ref_geometry"
+g++ "${flags[@]}" "$here/ref_drivers_main.cpp" "$obj"/*.o -L "$out" -lkvref -fopenmp \
+    -Wl,-rpath,'$ORIGIN' -o "$out/ref_drivers"
+rm -rf "$obj"
+echo "build_ref: built $out/ref_drivers"
 g++ -std=c++17 -O1 -w -fpermissive -include climits -I "$here/ref_vtk_stub" -I "$ref/source" \
     "$here/ref_histogram_driver.cpp" -o "$out/ref_histogram"
 echo "build_ref: built $out/ref_histogram"

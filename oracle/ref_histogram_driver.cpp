@@ -17,6 +17,7 @@
 static vtkSmartPointer<vtkImageData> load(const std::vector<unsigned short> &v, int nx, int ny, int nz) {
     auto im = vtkSmartPointer<vtkImageData>::New();
     im->SetDimensions(nx, ny, nz);
+    im->AllocateScalars(VTK_UNSIGNED_SHORT, 1);
     std::memcpy(im->GetScalarPointer(), v.data(), v.size() * sizeof(unsigned short));
     return im;
 }

@@ -1,5 +1,6 @@
 // Minimal stand-in for VTK's vtkSmartPointer (TEST INFRASTRUCTURE, beside
-// the vtkImageData stand-in): shared ownership, ->, comparison with nullptr.
+// the vtkImageData stand-in): shared ownership, ->, conversion to the raw
+// pointer, comparison with nullptr.
 #pragma once
 
 #include <memory>
@@ -12,6 +13,7 @@ public:
     static vtkSmartPointer New() { return vtkSmartPointer(T::New()); }
     T *operator->() const { return m_p.get(); }
     T *Get() const { return m_p.get(); }
+    operator T *() const { return m_p.get(); }
     friend bool operator==(const vtkSmartPointer &a, std::nullptr_t) { return a.m_p == nullptr; }
     friend bool operator!=(const vtkSmartPointer &a, std::nullptr_t) { return a.m_p != nullptr; }
 
