@@ -5,8 +5,14 @@
 // reference's uniform start (PhantomMaker, background 1), on the reference's
 // kernels compiled for the host (the Projector stand-in in ref_driver_shim/):
 //   ref_drivers <geometry.xml> <proj.raw> <mlem|art> <iterations> <relax> <out.raw>
-// writes the reconstructed volume [nz][ny][nx] as raw float32.
+// writes the reconstructed volume [nz][ny][nx] as raw float32;
+//   ref_drivers <geometry.xml> saa-shifts
+// runs recons::ShiftAndAdd (Reconstructors.h:263-379) over VTK filter
+// stand-ins that record the integer row shift the reference computes for
+// every slice and view and prints them, slice-major, as the last line of
+// output ({"status": "error"} when the reference refuses the geometry).
 // TEST INFRASTRUCTURE: the checker for the restated drivers of the oracle.
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <string>
@@ -14,13 +20,24 @@
 #include "modules/reconstruction/Reconstructors.h"
 
 int main(int argc, char **argv) {
-    if (argc != 7) return 2;
+    if (argc != 7 && !(argc == 3 && std::string(argv[2]) == "saa-shifts")) return 2;
     TomoGeometry geometry{std::string(argv[1])};
     if (!geometry.IsValid()) return 3;
     const auto roi = geometry.projectionsRoisSize();
     auto projections = vtkSmartPointer<vtkImageData>::New();
     projections->SetDimensions(roi.x, roi.y, geometry.nbProjectionsRois());
     projections->AllocateScalars(VTK_FLOAT, 1);
+    if (argc == 3) {
+        auto r = recons::ShiftAndAdd(&geometry, projections, std::nullopt);
+        if (r.has_error()) {
+            std::printf("\n{\"status\": \"error\"}\n");
+            return 0;
+        }
+        std::printf("\n{\"status\": \"ok\", \"shifts\": [");
+        for (size_t i = 0; i < vtk_recorded_shifts.size(); ++i) std::printf("%s%d", i ? ", " : "", vtk_recorded_shifts[i]);
+        std::printf("]}\n");
+        return 0;
+    }
     const size_t n = static_cast<size_t>(roi.x) * roi.y * geometry.nbProjectionsRois();
     std::ifstream(argv[2], std::ios::binary)
         .read(static_cast<char *>(projections->GetScalarPointer()), static_cast<std::streamsize>(n * 4));

@@ -1,10 +1,9 @@
-// Compile-only stand-in for VTK's vtkImageAppend (TEST INFRASTRUCTURE), see
-// vtk_unused_filter.h.
+// Stand-in for VTK's vtkImageAppend (TEST INFRASTRUCTURE), see vtk_recording_filter.h.
 #pragma once
 
-#include "vtk_unused_filter.h"
+#include "vtk_recording_filter.h"
 
-class vtkImageAppend : public vtkUnusedFilter {
+class vtkImageAppend : public vtkRecordingFilter {
 public:
     static vtkImageAppend *New() { return new vtkImageAppend; }
 };

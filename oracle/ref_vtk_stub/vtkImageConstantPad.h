@@ -1,10 +1,9 @@
-// Compile-only stand-in for VTK's vtkImageConstantPad (TEST INFRASTRUCTURE), see
-// vtk_unused_filter.h.
+// Stand-in for VTK's vtkImageConstantPad (TEST INFRASTRUCTURE), see vtk_recording_filter.h.
 #pragma once
 
-#include "vtk_unused_filter.h"
+#include "vtk_recording_filter.h"
 
-class vtkImageConstantPad : public vtkUnusedFilter {
+class vtkImageConstantPad : public vtkRecordingFilter {
 public:
     static vtkImageConstantPad *New() { return new vtkImageConstantPad; }
 };

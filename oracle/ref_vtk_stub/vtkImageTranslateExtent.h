@@ -1,10 +1,9 @@
-// Compile-only stand-in for VTK's vtkImageTranslateExtent (TEST INFRASTRUCTURE), see
-// vtk_unused_filter.h.
+// Stand-in for VTK's vtkImageTranslateExtent (TEST INFRASTRUCTURE), see vtk_recording_filter.h.
 #pragma once
 
-#include "vtk_unused_filter.h"
+#include "vtk_recording_filter.h"
 
-class vtkImageTranslateExtent : public vtkUnusedFilter {
+class vtkImageTranslateExtent : public vtkRecordingFilter {
 public:
     static vtkImageTranslateExtent *New() { return new vtkImageTranslateExtent; }
 };

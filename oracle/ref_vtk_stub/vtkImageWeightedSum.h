@@ -1,10 +1,9 @@
-// Compile-only stand-in for VTK's vtkImageWeightedSum (TEST INFRASTRUCTURE), see
-// vtk_unused_filter.h.
+// Stand-in for VTK's vtkImageWeightedSum (TEST INFRASTRUCTURE), see vtk_recording_filter.h.
 #pragma once
 
-#include "vtk_unused_filter.h"
+#include "vtk_recording_filter.h"
 
-class vtkImageWeightedSum : public vtkUnusedFilter {
+class vtkImageWeightedSum : public vtkRecordingFilter {
 public:
     static vtkImageWeightedSum *New() { return new vtkImageWeightedSum; }
 };

@@ -1,10 +1,9 @@
-// Compile-only stand-in for VTK's vtkTIFFWriter (TEST INFRASTRUCTURE), see
-// vtk_unused_filter.h.
+// Stand-in for VTK's vtkTIFFWriter (TEST INFRASTRUCTURE), see vtk_recording_filter.h.
 #pragma once
 
-#include "vtk_unused_filter.h"
+#include "vtk_recording_filter.h"
 
-class vtkTIFFWriter : public vtkUnusedFilter {
+class vtkTIFFWriter : public vtkRecordingFilter {
 public:
     static vtkTIFFWriter *New() { return new vtkTIFFWriter; }
 };

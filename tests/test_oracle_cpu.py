@@ -323,3 +323,40 @@ def test_rc_drivers_match_reference_drivers(tmp_path):
                             str(tmp_path / "x.raw")], check=True, capture_output=True)
             ref = np.fromfile(tmp_path / "x.raw", np.float32).reshape(g.volume_shape)
             assert np.array_equal(restated(g, p, np.ones(g.volume_shape, np.float32), 3, relax), ref), (method, relax)
+
+
+def test_rc_shift_rule_matches_reference_code():
+    """The row shifts of the RC shift-and-add -- the C ABI's rule
+    (kv_shift_and_add_shifts) and the oracle's -- against those the
+    reference's own recons::ShiftAndAdd computes (Reconstructors.h:287-331),
+    read back from its VTK filter calls by oracle/_ref/ref_drivers, on
+    geometry files read by the reference's reader: equal."""
+    import subprocess
+    import sys
+    import tempfile
+    from oracle import build as ob
+    from kevernals_gb300 import build as kb, engine
+    ob.build_ref()
+    if not (os.path.exists(ob.REF_DRIVERS) and os.path.exists(ob.REF_GEOMETRY)):
+        pytest.skip("reference drivers not built (needs the reference tree)")
+    kb.build()
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_geometry_xml import write_xml
+
+    def last(cmd):
+        out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
+        return json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+    with tempfile.TemporaryDirectory() as d:
+        xml = os.path.join(d, "geo.xml")
+        for kw in ({}, {"res": (8, 40, 36), "scale": (1.0, 0.5, 0.5), "roi": "30 20 0 0 79 59"},
+                   {"centre": (-3.5, 7.25, 12.0), "res": (7, 33, 21), "scale": (2.5, 0.4, 0.3), "views": 9},
+                   {"centre": (0.125, -250.0, 600.0), "res": (64, 16, 8), "scale": (0.7, 1.1, 0.9), "views": 4}):
+            write_xml(xml, **kw)
+            r = last([ob.REF_DRIVERS, xml, "saa-shifts"])
+            f = last([ob.REF_GEOMETRY, xml])
+            g = Geometry(*f["n"], *f["d"], *f["det"], *f["pitch"], np.asarray(f["src"], np.float32).reshape(-1, 3),
+                         np.asarray(f["det_origin"], np.float32).reshape(-1, 3), f["fulcrum_z"])
+            assert r["status"] == "ok"
+            ref = np.asarray(r["shifts"], np.int32).reshape(g.nz, g.n_views)
+            assert np.array_equal(engine.shift_and_add_shifts(g, "rc"), ref), kw
+            assert np.array_equal(O.saa_shifts(g, 0), ref), kw
