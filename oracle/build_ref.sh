@@ -22,7 +22,8 @@
 #                                    (libkvref.so) through the Projector
 #                                    stand-in in ref_driver_shim/ and the VTK
 #                                    stand-ins in ref_vtk_stub/ (those of the
-#                                    shift-and-add filters abort if called)
+#                                    shift-and-add filters compute nothing and
+#                                    record the shift rule's rows)
 #   oracle/_ref/ref_histogram        the reference's histogram tools
 #                                    (source/commons/HistogramMatchingTools.h)
 #                                    behind ref_histogram_driver.cpp, against
