@@ -9,6 +9,7 @@ import json
 import os
 import shutil
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -271,67 +272,80 @@ def test_geometry_accessors(dumper, tmp_path):
 
 # ---- against the reference's own reader ------------------------------------
 
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_ref_tools_golden as G  # noqa: E402
+
+
 @pytest.fixture(scope="module")
 def ref_reader():
     """The reference's XML reader (its geometry module and tinyxml2, compiled
-    from the reference tree by oracle/build_ref.sh); absent without the tree."""
+    from the reference tree by oracle/build_ref.sh), or None without the tree:
+    the tests then use the fixtures tests/golden/make_ref_tools_golden.py
+    recorded from it."""
     from oracle import build as ob
     ob.build_ref()
-    if not os.path.exists(ob.REF_GEOMETRY):
-        pytest.skip("reference geometry reader not built (needs the reference tree)")
-    return ob.REF_GEOMETRY
+    return ob.REF_GEOMETRY if os.path.exists(ob.REF_GEOMETRY) else None
 
 
-def _ref_read(ref_reader, *args):
-    out = subprocess.run([ref_reader, *args], check=True, capture_output=True, text=True).stdout
-    return json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+def _reference(ref_reader, key, args, reduce=False):
+    """The reference reader's output for `args`: run live when it is built
+    (the committed fixture must then agree with it), else the fixture."""
+    fix = G.load()
+    fixed = json.loads(str(fix[key])) if fix is not None and key in fix else None
+    if ref_reader is None:
+        if fixed is None:
+            pytest.skip("neither the reference reader nor its fixtures")
+        return fixed
+    live = json.loads(G.last_json([ref_reader, *args]))
+    if reduce:
+        live = G.reduce_lists(live)
+    assert fixed is None or live == fixed, f"{key}: tests/golden/golden_ref_tools.npz is stale"
+    return live
 
 
-VARIANTS = [
-    {},
-    {"centre": (-3.5, 7.25, 12.0), "res": (7, 33, 21), "scale": (2.5, 0.4, 0.3), "views": 9,
-     "roi": "0 0 0 0 99 74"},
-    {"roi": "-5 3 0 0 150 90"},                     # corners clamped to the detector
-    {"views": 1, "roi": "40 30 0 0 40 30"},          # one view, a one-pixel ROI
-    {"centre": (0.125, -250.0, 600.0), "res": (64, 16, 8), "scale": (0.7, 1.1, 0.9), "views": 4},
-]
+def _same(ours, ref, keys):
+    for k in keys:
+        a, b = ours[k], ref[k]
+        if isinstance(b, list) and b and isinstance(b[0], float):
+            assert np.array_equal(np.asarray(a, np.float32), np.asarray(b, np.float32)), k
+        else:
+            assert a == b, k
 
 
-@pytest.mark.parametrize("i", range(len(VARIANTS)))
+@pytest.mark.parametrize("i", range(len(G.VARIANTS)))
 def test_xml_reader_matches_reference_reader(dumper, ref_reader, tmp_path, i):
     """The drop-in's reader and the reference's own reader on the same files:
     what the projector receives is equal bit for bit."""
     path = str(tmp_path / "geo.xml")
-    write_xml(path, **VARIANTS[i])
-    ours, ref = read(dumper, path), _ref_read(ref_reader, path)
+    write_xml(path, **G.VARIANTS[i])
+    ours, ref = read(dumper, path), _reference(ref_reader, f"xml_flat_{i}", [path])
     assert ours["valid"] and ref["valid"], (ours, ref)
-    for k in ("n", "views", "det"):
-        assert ours[k] == ref[k], k
-    for k in ("d", "pitch", "src", "det_origin", "fulcrum_z"):
-        assert np.array_equal(np.asarray(ours[k], np.float32), np.asarray(ref[k], np.float32)), k
+    assert np.float32(ours["fulcrum_z"]) == np.float32(ref["fulcrum_z"])
+    _same(ours, ref, ("n", "views", "det", "d", "pitch", "src", "det_origin"))
 
 
-@pytest.mark.parametrize("args", [("accessors",), ("adapt", "3", "0", "9", "3", "accessors")])
-def test_xml_accessors_match_reference_reader(dumper, ref_reader, tmp_path, args):
+@pytest.mark.parametrize("j", range(len(G.ACCESSOR_ARGS)))
+def test_xml_accessors_match_reference_reader(dumper, ref_reader, tmp_path, j):
     """Every value accessor, before and after the demonstration adaptation,
-    equal to the reference reader's."""
+    equal to the reference reader's (long position lists compared through
+    the SHA-256 of their float32 values)."""
     path = str(tmp_path / "geo.xml")
-    write_xml(path, res=(3, 4, 5), roi="1 2 0 0 6 5")
-    ours = json.loads(subprocess.run([dumper, path, *args], check=True, capture_output=True, text=True).stdout)
-    ref = _ref_read(ref_reader, path, *args)
+    write_xml(path, **G.ACCESSOR_XML)
+    args = G.ACCESSOR_ARGS[j]
+    ours = G.reduce_lists(json.loads(subprocess.run([dumper, path, *args], check=True, capture_output=True,
+                                                    text=True).stdout))
+    ref = _reference(ref_reader, f"xml_acc_{j}", [path, *args], reduce=True)
     assert set(ours) == set(ref)
-    for k, v in ref.items():
-        if isinstance(v, list) and v and isinstance(v[0], float) or k.endswith(("wsize", "pitch", "size")):
-            assert np.array_equal(np.asarray(ours[k], np.float32), np.asarray(v, np.float32)), k
-        else:
-            assert ours[k] == v, k
+    _same(ours, ref, sorted(ref))
 
 
 def test_xml_invalid_files_match_reference_reader(dumper, ref_reader, tmp_path):
     """Files both readers refuse: a missing section, ROIs that differ between
-    views, a truncated file."""
+    views (run live only)."""
+    if ref_reader is None:
+        pytest.skip("reference reader not built (needs the reference tree)")
     path = str(tmp_path / "bad.xml")
     for kw in ({"drop": "Grid"}, {"drop": "Rotation"},
                {"rois": ["10 20 0 0 89 79"] * 2 + ["11 20 0 0 89 79"] + ["10 20 0 0 89 79"] * 2}):
         write_xml(path, **kw)
-        assert not read(dumper, path)["valid"] and not _ref_read(ref_reader, path)["valid"], kw
+        assert not read(dumper, path)["valid"] and not json.loads(G.last_json([ref_reader, path]))["valid"], kw

@@ -292,71 +292,83 @@ np.savez({str(tmp_path / "asan.npz")!r}, *out)
         i += 9
 
 
+def _ref_tools():
+    """(fixture module, fixtures or None, live checkers built?)"""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import make_ref_tools_golden as G
+    from oracle import build as ob
+    ob.build_ref()
+    live = os.path.exists(ob.REF_DRIVERS) and os.path.exists(ob.REF_GEOMETRY)
+    fix = G.load()
+    if not live and fix is None:
+        pytest.skip("neither the reference checkers nor their fixtures")
+    return G, fix, live, ob
+
+
 def test_rc_drivers_match_reference_drivers(tmp_path):
     """The oracle's restated ART and MLEM (the drivers the engine's RC path
     reproduces bit for bit) against the reference's own drivers --
     recons::ART / recons::MLEM of Reconstructors.h with PhantomMaker's uniform
     start, compiled from the reference tree and run on the reference's
-    kernels built for the host (oracle/_ref/ref_drivers) -- on a geometry read
-    by the reference's reader, with rays that miss the volume: equal bit for
-    bit, for 3 iterations at relax 0.5 and 1.0."""
+    kernels built for the host (oracle/_ref/ref_drivers), or the digests of
+    their results committed in tests/golden -- on a geometry read by the
+    reference's reader, with rays that miss the volume: equal bit for bit,
+    for 3 iterations at relax 0.5 and 1.0."""
     import subprocess
-    import sys
-    from oracle import build as ob
-    ob.build_ref()
-    if not (os.path.exists(ob.REF_DRIVERS) and os.path.exists(ob.REF_GEOMETRY)):
-        pytest.skip("reference drivers not built (needs the reference tree)")
-    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    G, fix, live, ob = _ref_tools()
     from test_geometry_xml import write_xml
     xml = str(tmp_path / "geo.xml")
-    write_xml(xml, res=(8, 40, 36), scale=(1.0, 0.5, 0.5), roi="30 20 0 0 79 59")
-    out = subprocess.run([ob.REF_GEOMETRY, xml], capture_output=True, text=True, check=True).stdout
-    f = json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
-    g = Geometry(*f["n"], *f["d"], *f["det"], *f["pitch"], np.asarray(f["src"], np.float32).reshape(-1, 3),
-                 np.asarray(f["det_origin"], np.float32).reshape(-1, 3), f["fulcrum_z"])
-    p = O.rc_forward(g, O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 6, 9)))
+    write_xml(xml, **G.DRIVER_CASE["xml"])
+    if live:
+        flat = G.last_json([ob.REF_GEOMETRY, xml])
+        assert fix is None or json.loads(flat) == json.loads(str(fix["drv_geometry"])), "stale fixtures"
+    else:
+        flat = str(fix["drv_geometry"])
+    g, p = G.driver_inputs(flat=flat)
     assert 0 < np.count_nonzero(p) < p.size           # some rays miss the volume
     p.tofile(tmp_path / "proj.raw")
     for method, restated in (("mlem", O.rc_mlem), ("art", O.rc_art)):
         for relax in (0.5, 1.0):
-            subprocess.run([ob.REF_DRIVERS, xml, str(tmp_path / "proj.raw"), method, "3", str(relax),
-                            str(tmp_path / "x.raw")], check=True, capture_output=True)
-            ref = np.fromfile(tmp_path / "x.raw", np.float32).reshape(g.volume_shape)
-            assert np.array_equal(restated(g, p, np.ones(g.volume_shape, np.float32), 3, relax), ref), (method, relax)
+            ours = G.digest(restated(g, p, np.ones(g.volume_shape, np.float32), G.DRIVER_CASE["iterations"], relax))
+            key = f"drv_{method}_{relax}"
+            if live:
+                subprocess.run([ob.REF_DRIVERS, xml, str(tmp_path / "proj.raw"), method,
+                                str(G.DRIVER_CASE["iterations"]), str(relax), str(tmp_path / "x.raw")],
+                               check=True, capture_output=True)
+                ref = G.digest(np.fromfile(tmp_path / "x.raw", np.float32))
+                assert fix is None or str(fix[key]) == ref, f"{key}: stale fixtures"
+            else:
+                ref = str(fix[key])
+            assert ours == ref, (method, relax)
 
 
-def test_rc_shift_rule_matches_reference_code():
+def test_rc_shift_rule_matches_reference_code(tmp_path):
     """The row shifts of the RC shift-and-add -- the C ABI's rule
     (kv_shift_and_add_shifts) and the oracle's -- against those the
     reference's own recons::ShiftAndAdd computes (Reconstructors.h:287-331),
-    read back from its VTK filter calls by oracle/_ref/ref_drivers, on
-    geometry files read by the reference's reader: equal."""
-    import subprocess
-    import sys
-    import tempfile
-    from oracle import build as ob
+    read back from its VTK filter calls by oracle/_ref/ref_drivers (or their
+    committed fixtures), on geometry files read by the reference's reader:
+    equal."""
     from kevernals_gb300 import build as kb, engine
-    ob.build_ref()
-    if not (os.path.exists(ob.REF_DRIVERS) and os.path.exists(ob.REF_GEOMETRY)):
-        pytest.skip("reference drivers not built (needs the reference tree)")
+    G, fix, live, ob = _ref_tools()
     kb.build()
-    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     from test_geometry_xml import write_xml
-
-    def last(cmd):
-        out = subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
-        return json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
-    with tempfile.TemporaryDirectory() as d:
-        xml = os.path.join(d, "geo.xml")
-        for kw in ({}, {"res": (8, 40, 36), "scale": (1.0, 0.5, 0.5), "roi": "30 20 0 0 79 59"},
-                   {"centre": (-3.5, 7.25, 12.0), "res": (7, 33, 21), "scale": (2.5, 0.4, 0.3), "views": 9},
-                   {"centre": (0.125, -250.0, 600.0), "res": (64, 16, 8), "scale": (0.7, 1.1, 0.9), "views": 4}):
+    xml = str(tmp_path / "geo.xml")
+    for k, kw in enumerate(G.SHIFT_CASES):
+        if live:
             write_xml(xml, **kw)
-            r = last([ob.REF_DRIVERS, xml, "saa-shifts"])
-            f = last([ob.REF_GEOMETRY, xml])
-            g = Geometry(*f["n"], *f["d"], *f["det"], *f["pitch"], np.asarray(f["src"], np.float32).reshape(-1, 3),
-                         np.asarray(f["det_origin"], np.float32).reshape(-1, 3), f["fulcrum_z"])
+            flat = G.last_json([ob.REF_GEOMETRY, xml])
+            r = json.loads(G.last_json([ob.REF_DRIVERS, xml, "saa-shifts"]))
             assert r["status"] == "ok"
-            ref = np.asarray(r["shifts"], np.int32).reshape(g.nz, g.n_views)
-            assert np.array_equal(engine.shift_and_add_shifts(g, "rc"), ref), kw
-            assert np.array_equal(O.saa_shifts(g, 0), ref), kw
+            ref = np.asarray(r["shifts"], np.int32)
+            if fix is not None:
+                assert json.loads(flat) == json.loads(str(fix[f"shift_geometry_{k}"])), "stale fixtures"
+                assert np.array_equal(ref.reshape(fix[f"shifts_{k}"].shape), fix[f"shifts_{k}"]), "stale fixtures"
+        else:
+            flat, ref = str(fix[f"shift_geometry_{k}"]), fix[f"shifts_{k}"]
+        g = G.geometry_from_flat(json.loads(flat))
+        ref = np.asarray(ref, np.int32).reshape(g.nz, g.n_views)
+        assert np.array_equal(engine.shift_and_add_shifts(g, "rc"), ref), kw
+        assert np.array_equal(O.saa_shifts(g, 0), ref), kw

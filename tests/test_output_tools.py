@@ -121,30 +121,37 @@ def test_rescale_handles_non_finite_voxels(tool, tmp_path):
 def test_histogram_tools_match_reference(tool, tmp_path):
     """HistUniformization16Bit / HistHalfTop16Bit of the drop-in against the
     reference's own header (HistogramMatchingTools.h, compiled from the
-    reference tree by oracle/build_ref.sh) on the same 16-bit images: a
-    rescaled gamma volume with a zero (masked) patch, a few-level image, and
-    an image with one non-zero level.  Equal bit for bit."""
+    reference tree by oracle/build_ref.sh, or its results committed in
+    tests/golden) on the same 16-bit images: a rescaled gamma volume with a
+    zero (masked) patch, a few-level image, and an image with one non-zero
+    level.  Equal bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_ref_tools_golden as G
     from oracle import build as ob
     ob.build_ref()
-    if not os.path.exists(ob.REF_HISTOGRAM):
-        pytest.skip("reference histogram tools not built (needs the reference tree)")
-    rng = np.random.default_rng(11)
-    nx, ny, nz = 29, 17, 3
-    gamma = rng.gamma(2.0, 0.01, size=(nz, ny, nx)).astype(np.float32)
-    gamma[0, :4, :5] = 0.0
-    levels = rng.integers(0, 4, size=(nz, ny, nx)).astype(np.float32) * 0.25
-    single = np.zeros((nz, ny, nx), np.float32)
-    single[1, 5:9, 3:12] = 1.0
-    for k, vol in enumerate((gamma, levels, single)):
+    live = os.path.exists(ob.REF_HISTOGRAM)
+    fix = G.load()
+    if not live and fix is None:
+        pytest.skip("neither the reference histogram tools nor their fixtures")
+    nz, ny, nx = G.HIST_SHAPE
+    for k, vol in enumerate(G.hist_cases()):
         case = tmp_path / f"case{k}"
         case.mkdir()
         vol.tofile(case / "vol.raw")
         subprocess.run([tool, str(case / "vol.raw"), str(nx), str(ny), str(nz), str(case)], check=True)
-        ref = case / "ref"
-        ref.mkdir()
-        subprocess.run([ob.REF_HISTOGRAM, str(case / "u16.raw"), str(nx), str(ny), str(nz), str(ref) + "/"],
-                       check=True)
         u16 = np.fromfile(case / "u16.raw", np.uint16)
-        assert np.array_equal(np.fromfile(ref / "hist.raw", np.int32), np.bincount(u16, minlength=65536))
-        for name in ("uniform.raw", "halftop.raw"):
-            assert np.array_equal(np.fromfile(case / name, np.uint16), np.fromfile(ref / name, np.uint16)), (k, name)
+        assert np.array_equal(u16, rescale_u16(vol).ravel())
+        if live:
+            ref = case / "ref"
+            ref.mkdir()
+            subprocess.run([ob.REF_HISTOGRAM, str(case / "u16.raw"), str(nx), str(ny), str(nz), str(ref) + "/"],
+                           check=True)
+            assert np.array_equal(np.fromfile(ref / "hist.raw", np.int32), np.bincount(u16, minlength=65536))
+        for name in ("uniform", "halftop"):
+            if live:
+                expect = np.fromfile(ref / f"{name}.raw", np.uint16)
+                assert fix is None or np.array_equal(fix[f"hist_{k}_{name}"].ravel(), expect), "stale fixtures"
+            else:
+                expect = fix[f"hist_{k}_{name}"].ravel()
+            assert np.array_equal(np.fromfile(case / f"{name}.raw", np.uint16), expect), (k, name)
