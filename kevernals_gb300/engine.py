@@ -95,6 +95,13 @@ class Context:
             lib().kv_ctx_destroy(self._h)
             self._h = None
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
+
     def __del__(self):
         if sys.is_finalizing():
             return
@@ -138,6 +145,13 @@ class Plan:
         if getattr(self, "_h", None):
             lib().kv_plan_destroy(self._h)
             self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
 
     def __del__(self):
         if sys.is_finalizing():
@@ -371,6 +385,13 @@ class UNet:
         if getattr(self, "_h", None):
             lib().kv_unet_destroy(self._h)
             self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
 
     def __del__(self):
         if sys.is_finalizing():

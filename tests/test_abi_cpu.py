@@ -219,3 +219,14 @@ for bad in (dataclasses.replace(g, fulcrum_z=float("nan")), dataclasses.replace(
                UBSAN_OPTIONS="halt_on_error=1")
     r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, env=env, timeout=600)
     assert r.returncode == 0 and "ERROR" not in r.stderr and "runtime error" not in r.stderr, r.stderr[-3000:]
+
+
+def test_python_handles_are_context_managers():
+    """Context, Plan and UNet close their handles on leaving a with block
+    (checked on a stand-in handle: creating one needs a GPU)."""
+    for cls in (engine.Context, engine.Plan, engine.UNet):
+        obj = cls.__new__(cls)
+        obj._h = None                       # nothing to destroy
+        with obj as same:
+            assert same is obj
+        assert obj._h is None
