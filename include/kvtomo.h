@@ -99,6 +99,12 @@ typedef struct kv_plan kv_plan;
 typedef int (*kv_iter_cb)(int iteration, double residual, double loglik, void *user);
 
 /* ---- library / context ------------------------------------------------ */
+/* No reference counterpart as functions: the reference uses the CUDA
+ * default device and stream implicitly and exits on a CUDA error
+ * (checkCudaErrors, CudaErrorHandler.h:581-594).  A context makes the
+ * device and stream explicit; kv_status, kv_status_string and
+ * kv_ctx_last_error replace that exit (and play the part of the
+ * Result<T> / std::error_code convention, Result.h:17-41). */
 const char *kv_version(void);
 const char *kv_status_string(kv_status s);
 kv_status kv_ctx_create(int device, kv_ctx **out);
@@ -120,7 +126,10 @@ kv_status kv_ctx_timing_read(kv_ctx *ctx, char *buf, size_t buflen);
 
 /* ---- plans -------------------------------------------------------------- */
 /* Validates the geometry, uploads per-view tables, and keeps the workspace a
- * solve needs.  The geometry arrays are copied; the caller may free them. */
+ * solve needs.  The geometry arrays are copied; the caller may free them.
+ * Replaces the geometry flattening and device set-up that
+ * Projector::PerformProjection / PerformBackProjection repeat on every call
+ * (Projector.cu:873-954, 1038-1125): here they are done once per plan. */
 kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *geom, kv_family family,
                          kv_storage storage, kv_plan **out);
 kv_status kv_plan_destroy(kv_plan *plan);
