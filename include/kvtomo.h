@@ -216,6 +216,19 @@ kv_status kv_plan_autotune(kv_plan *plan);
 kv_status kv_plan_get_tuning(const kv_plan *plan, int *fwd_rows, int *back_rows);
 kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_rows);
 
+/* Shape of the slab-staged EXACT forward projector (no reference
+ * counterpart; it replaces the per-pixel-thread CudaPerformProjection,
+ * Projector.cu:227-372, on the EXACT path): CTAs of 32 x 8*rays_per_thread
+ * detector rays, the volume staged `slices` slices at a time in shared
+ * memory with `stages` slabs in flight, `view_group` consecutive views
+ * launched together.  rays_per_thread = 0 selects the one-thread-per-ray
+ * kernel.  Plans take a default shape when their geometry suits it (at most
+ * two column and four row planes crossed per ray and slice); set returns
+ * KV_ERR_UNSUPPORTED with a reason when a shape does not fit the geometry.
+ * get reports rays_per_thread = 0 when the plan runs the per-ray kernel. */
+kv_status kv_plan_get_slab(const kv_plan *plan, int *rays_per_thread, int *slices, int *stages, int *view_group);
+kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int slices, int stages, int view_group);
+
 /* ---- learned warm start (no reference counterpart) ----------------------
  * A 3D U-Net (4 levels, 16/32/64/128 channels, 3x3x3 convolutions, BF16
  * weights and activations, FP32 accumulation, tensor-core implicit-GEMM
@@ -256,12 +269,18 @@ kv_status kv_residual(kv_plan *plan, const float *projections, const float *volu
  * device pointers; the results are written to the two host doubles.
  * Scratch: a static device array of KV_NOALLOC_MAX_BLOCKS FP64 partial-sum
  * triples (1.5 MiB) that every GPU loading the library holds until the
- * process exits; a geometry whose forward projection needs more blocks than
- * that (ceil(nu/32) * ceil(nv/4) * n_views > KV_NOALLOC_MAX_BLOCKS) is
- * rejected with KV_ERR_INVALID_ARG -- use kv_residual for it.  The first call
- * on a device looks up the array's device address, so make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on one GPU race and must be serialised by the caller. */
+ * process exits.  The residual runs the one-thread-per-ray forward kernel in
+ * blocks of 32 x fwd_rows rays, fwd_rows being the plan's forward block
+ * height (kv_plan_get_tuning: 4 unless kv_plan_set_tuning or
+ * kv_plan_autotune changed it, at most 8); a geometry with
+ *     ceil(nu / 32) * ceil(nv / fwd_rows) * n_views > KV_NOALLOC_MAX_BLOCKS
+ * is rejected with KV_ERR_INVALID_ARG -- use kv_residual for it.  The first
+ * call on a device looks up the array's device address and keeps it for the
+ * life of that device's primary context (do not call this entry point again
+ * after resetting the device in the same process); make that first call
+ * before any stream capture.  The call leaves the caller's current device as
+ * it found it.  All calls share the array: calls that overlap on one GPU race
+ * and must be serialised by the caller. */
 #define KV_NOALLOC_MAX_BLOCKS 65536
 kv_status kv_residual_noalloc(kv_plan *plan, const float *projections, const float *volume,
                               double *rel_residual, double *loglik);

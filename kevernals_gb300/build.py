@@ -25,6 +25,7 @@ SOURCES = {
     "kv_exact.cu": [],
     "kv_rc.cu": ["-fmad=false"],
     "kv_misc.cu": [],
+    "kv_fwd_slab.cu": [],
     "kv_unet.cu": [],
 }
 

@@ -27,11 +27,28 @@ kv_status kv_fail(kv_ctx *ctx, kv_status s, const char *fmt, ...) {
 
 namespace {
 
-// Reduction helpers (kv_reduce.cu)
+bool stream_capturing(kv_ctx *ctx);
+
+// Error bits that self-checking kernels leave in ctx->d_status (a bounded
+// wait that gave up, a ray outside its staged box), read at the points where
+// the call synchronises anyway, cleared, and returned as a status.
+kv_status device_status(kv_ctx *ctx) {
+    if (ctx->d_status == nullptr || stream_capturing(ctx)) return KV_OK;
+    int h = 0;
+    KV_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_status, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h == 0) return KV_OK;
+    KV_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+    return kv_fail(ctx, (h & 1) ? KV_ERR_TIMEOUT : KV_ERR_CUDA,
+                   "a projector kernel stopped early (status bits 0x%x: 1 = a staged load did not arrive, "
+                   "2/4 = a ray left its staged box)", h);
+}
+
 kv_status residual_from_red(kv_ctx *ctx, double *res, double *ll) {
     double h[3];
     KV_CHECK_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_red, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    KV_TRY(device_status(ctx));
     if (res) *res = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
     if (ll) *ll = h[2];
     return KV_OK;
@@ -65,7 +82,7 @@ kv_status stage_out(kv_plan *plan, float *user, kv_mem mem, const float *dev, si
     KV_CHECK_CUDA(plan->ctx, cudaMemcpyAsync(user, dev, n * sizeof(float), cudaMemcpyDeviceToHost,
                                              plan->ctx->stream));
     KV_CHECK_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
-    return KV_OK;
+    return device_status(plan->ctx);
 }
 
 kv_status check_common(kv_plan *plan, const void *a, const void *b, kv_mem mem) {
@@ -209,7 +226,7 @@ kv_status sync_both(kv_ctx *ctx, kv_status s) {
     if (s != KV_OK) return s;
     if (e1 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e1));
     if (e2 != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "stream: %s", cudaGetErrorString(e2));
-    return KV_OK;
+    return device_status(ctx);
 }
 
 bool stream_capturing(kv_ctx *ctx) {
@@ -259,7 +276,11 @@ extern "C" kv_status kv_ctx_create(int device, kv_ctx **out) {
     ctx->sm_count = prop.multiProcessorCount;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc((void **)&ctx->d_red, 8 * sizeof(double)) != cudaSuccess) {
+        cudaMalloc((void **)&ctx->d_red, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->d_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(ctx->d_status, 0, sizeof(int)) != cudaSuccess) {
+        cudaFree(ctx->d_red);
+        cudaFree(ctx->d_status);
         if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
         delete ctx;
         return KV_ERR_CUDA;
@@ -282,6 +303,7 @@ void ctx_free(kv_ctx *ctx) {
     for (cudaEvent_t e : ctx->copy_events) cudaEventDestroy(e);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     cudaFree(ctx->d_red);
+    cudaFree(ctx->d_status);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -306,7 +328,7 @@ extern "C" kv_status kv_ctx_set_stream(kv_ctx *ctx, void *stream) {
 extern "C" kv_status kv_sync(kv_ctx *ctx) {
     if (ctx == nullptr) return KV_ERR_INVALID_ARG;
     KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return KV_OK;
+    return device_status(ctx);
 }
 
 extern "C" const char *kv_ctx_last_error(const kv_ctx *ctx) {
@@ -414,7 +436,18 @@ extern "C" kv_status kv_plan_create(kv_ctx *ctx, const kv_geometry *g, kv_family
     plan->nproj = (size_t)g->nu * g->nv * g->n_views;
     kv_status s = KV_OK;
     if (family == KV_FAMILY_EXACT) {
-        s = exact_build_tables(plan, plan->src.data(), plan->det.data(), g->n_views, &plan->ex);
+        s = exact_build_tables(plan, plan->src.data(), plan->det.data(), g->n_views, &plan->ex, &plan->hx);
+        // the slab-staged forward projector where the geometry suits it: the
+        // first shape of this list that fits (measured fastest first at the
+        // chest-DT geometry; kv_plan_autotune can pick another)
+        static const int shapes[][3] = {{8, 4, 2}, {4, 4, 3}, {4, 2, 3}, {2, 4, 3}, {2, 2, 2}};
+        for (const auto &sh : shapes) {
+            FwdSlabCfg c;
+            if (s == KV_OK && fwd_slab_fit(plan, sh[0], sh[1], sh[2], fwd_slab_default_group(g->n_views), &c, nullptr)) {
+                plan->fslab = c;
+                break;
+            }
+        }
     } else {
         size_t bytes = 3 * sizeof(float) * g->n_views;
         if (cudaMalloc((void **)&plan->d_src, bytes) != cudaSuccess ||
@@ -518,8 +551,13 @@ extern "C" kv_status kv_forward_single(kv_plan *plan, const float *volume, const
     } else {
         if (plan->storage != KV_STORAGE_F32) return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "single-view forward is FP32 only");
         ExactTables t;
-        KV_TRY(exact_build_tables(plan, src, det_origin, 1, &t));
+        KV_TRY(exact_build_tables(plan, src, det_origin, 1, &t, nullptr));
+        // the plan's slab boxes are sized for its own views: this view takes
+        // the one-thread-per-ray kernel
+        const FwdSlabCfg keep = plan->fslab;
+        plan->fslab.R = 0;
         kv_status s = exact_forward_launch(plan, t, 1, FWD_PLAIN, FwdArgs{vd, nullptr, pd, nullptr, 1.f});
+        plan->fslab = keep;
         cudaStreamSynchronize(plan->ctx->stream);
         exact_free_tables(&t);
         KV_TRY(s);
@@ -688,11 +726,16 @@ kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax,
 // as a CUDA graph on the context's own stream and launched on the call's
 // stream; the executable graph is kept and relaunched while the buffers and
 // parameters stay the same.
+long long slab_key(const FwdSlabCfg &c) {
+    return (((long long)c.R * 16 + c.S) * 8 + c.stages) * 65536 + c.group;
+}
+
 kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float relax, bool mlem) {
     kv_ctx *ctx = plan->ctx;
     const bool same = plan->graph_exec != nullptr && plan->graph_p == p && plan->graph_x == x &&
                       plan->graph_iters == iters && plan->graph_mlem == (int)mlem && plan->graph_relax == relax &&
-                      plan->graph_fb == plan->fwd_by && plan->graph_bb == plan->back_by;
+                      plan->graph_fb == plan->fwd_by && plan->graph_bb == plan->back_by &&
+                      plan->graph_slab == slab_key(plan->fslab);
     if (!same) {
         if (plan->graph_exec != nullptr) {
             KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -724,6 +767,7 @@ kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float 
         plan->graph_relax = relax;
         plan->graph_fb = plan->fwd_by;
         plan->graph_bb = plan->back_by;
+        plan->graph_slab = slab_key(plan->fslab);
     }
     KV_CHECK_CUDA(ctx, cudaGraphLaunch(plan->graph_exec, ctx->stream));
     return KV_OK;
@@ -960,5 +1004,32 @@ extern "C" kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_ro
         return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "tuning out of range (1..8 rows of 32 threads)");
     plan->fwd_by = fwd_rows;
     plan->back_by = back_rows;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_get_slab(const kv_plan *plan, int *rays_per_thread, int *slices, int *stages,
+                                      int *view_group) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (rays_per_thread) *rays_per_thread = plan->fslab.R;
+    if (slices) *slices = plan->fslab.S;
+    if (stages) *stages = plan->fslab.stages;
+    if (view_group) *view_group = plan->fslab.group;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int slices, int stages, int view_group) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (plan->family != KV_FAMILY_EXACT)
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "the slab forward projector is an EXACT-family kernel");
+    if (rays_per_thread == 0) {
+        plan->fslab = FwdSlabCfg{};
+        return KV_OK;
+    }
+    FwdSlabCfg c;
+    std::string why;
+    if (!fwd_slab_fit(plan, rays_per_thread, slices, stages, view_group, &c, &why))
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "slab shape (%d, %d, %d, %d) does not fit: %s",
+                       rays_per_thread, slices, stages, view_group, why.c_str());
+    plan->fslab = c;
     return KV_OK;
 }

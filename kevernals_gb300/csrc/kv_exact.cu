@@ -21,25 +21,13 @@
 // uses is bit-identical to the one the forward projector uses: A^T is the
 // exact transpose of A up to the order of the sums.
 #include "kv_internal.h"
+#include "kv_exact_common.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <mutex>
 
 namespace {
-
-struct ExGeom {
-    int nx, ny, nz, nu, nv, n_views;
-};
-
-__device__ __forceinline__ float cross_t(int rel_plane, float ft, float ix) {
-    return __fmul_rn(__fsub_rn((float)rel_plane, ft), ix);
-}
-
-// Ls = sqrt(ax^2 + ay^2 + H^2) * dz / H : length of the ray inside one slice.
-__device__ __forceinline__ float ray_factor(float ax, float ay, float4 vi) {
-    return __fmul_rn(__fsqrt_rn(__fadd_rn(__fmaf_rn(ax, ax, __fmul_rn(ay, ay)), vi.x)), vi.y);
-}
 
 // Range [k0, k1] of slices in which the ray may be inside the volume laterally.
 __device__ __forceinline__ void lateral_slices(float pos0, float slope, int n, int nz, float &klo,
@@ -469,7 +457,7 @@ void exact_free_tables(ExactTables *t) {
 }
 
 kv_status exact_build_tables(kv_plan *plan, const float *src, const float *det, int P,
-                             ExactTables *out) {
+                             ExactTables *out, ExactHostTables *host) {
     const kv_geometry &g = plan->g;
     kv_ctx *ctx = plan->ctx;
     const double X0 = -0.5 * g.nx * (double)g.dx, Y0 = -0.5 * g.ny * (double)g.dy;
@@ -536,6 +524,13 @@ kv_status exact_build_tables(kv_plan *plan, const float *src, const float *det, 
     }
     KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *out = t;
+    if (host != nullptr) {
+        host->xt = std::move(xt);
+        host->xi = std::move(xi);
+        host->yt = std::move(yt);
+        host->yi = std::move(yi);
+        host->hr = std::move(hr);
+    }
     return KV_OK;
 }
 
@@ -591,14 +586,17 @@ kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool ka
 kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
                                const FwdArgs &a) {
     if (plan->fwd_by < 1 || plan->fwd_by > 8) return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad forward block");
+    const bool slab = plan->fslab.R > 0;
     double *partials = nullptr;
     size_t nblocks = 0;
     if (a.red != nullptr) {
-        nblocks = (size_t)((plan->g.nu + 31) / 32) * ((plan->g.nv + plan->fwd_by - 1) / plan->fwd_by) * P;
+        nblocks = slab ? fwd_slab_blocks(plan, P)
+                       : (size_t)((plan->g.nu + 31) / 32) * ((plan->g.nv + plan->fwd_by - 1) / plan->fwd_by) * P;
         KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&partials, nblocks * 3 * sizeof(double), plan->ctx->stream));
     }
     kv_status s;
-    switch (plan->storage) {
+    if (slab) s = fwd_slab_launch(plan, t, P, mode, a, partials);
+    else switch (plan->storage) {
     case KV_STORAGE_BF16: s = fwd_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, t, P, mode, a, partials); break;
     case KV_STORAGE_F16: s = fwd_dispatch<__half, __half>(plan, t, P, mode, a, partials); break;
     default: s = fwd_dispatch<float, float>(plan, t, P, mode, a, partials); break;
@@ -708,7 +706,9 @@ static __device__ __align__(256) double g_noalloc_scratch[3 * KV_NOALLOC_MAX_BLO
 
 namespace {
 std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[64] = {};   // device address of g_noalloc_scratch, per device ordinal
+// Device address of g_noalloc_scratch, per device ordinal: valid for the life
+// of that device's primary context (the library never resets a device).
+double *g_noalloc_ptr[64] = {};
 
 // Set-up, once per device, with that device current: the host-side name of a
 // __device__ array is not a device address; ask the runtime for it.
@@ -744,7 +744,14 @@ extern "C" kv_status kv_residual_noalloc(kv_plan *plan, const float *projections
                        "kv_residual_noalloc: this geometry needs %zu partial sums but the static scratch holds "
                        "%d (at most %d forward blocks of 32 x %d rays); use kv_residual",
                        nblocks, KV_NOALLOC_MAX_BLOCKS, KV_NOALLOC_MAX_BLOCKS, by);
+    int caller_device = 0;
+    KV_CHECK_CUDA(ctx, cudaGetDevice(&caller_device));
     KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    // the caller's current device is put back on every path out
+    struct RestoreDevice {
+        int dev;
+        ~RestoreDevice() { cudaSetDevice(dev); }
+    } restore{caller_device};
     double *scratch = nullptr;
     KV_TRY(noalloc_scratch(ctx, &scratch));
     double *partials = scratch, *sums = scratch + 3 * (size_t)KV_NOALLOC_MAX_BLOCKS;

@@ -28,6 +28,7 @@ struct kv_ctx {
     cudaStream_t own_stream = nullptr;
     std::string last_error;
     double *d_red = nullptr;         // 8 doubles for FP64 reductions
+    int *d_status = nullptr;         // error bits set by kernels that check themselves (0: fine)
     // lifetime: plans hold a reference; kv_ctx_destroy only releases the
     // caller's, the context is freed with its last plan
     int plans = 0;
@@ -74,6 +75,25 @@ struct ExactTables {
     float4 *rng = nullptr;
 };
 
+// Host copies of the same tables (the slab forward projector sizes its
+// shared-memory boxes from them with the kernel's own float arithmetic).
+struct ExactHostTables {
+    std::vector<float4> xt, yt;
+    std::vector<int> xi, yi;
+    std::vector<float> hr;
+};
+
+// Launch shape of the slab-staged EXACT forward projector (kv_fwd_slab.cu);
+// R == 0: the plan uses the one-thread-per-ray kernel instead.
+struct FwdSlabCfg {
+    int R = 0;          // rays per thread along v: a CTA covers 32 x 8R rays
+    int S = 0;          // slices per slab
+    int stages = 0;     // slab boxes in flight
+    int group = 0;      // consecutive views launched together (L2 reuse)
+    int BX = 0, BY = 0; // box extent in voxels
+    size_t smem = 0;    // dynamic shared memory per CTA
+};
+
 struct kv_plan {
     kv_ctx *ctx = nullptr;
     kv_geometry g{};
@@ -84,6 +104,8 @@ struct kv_plan {
 
     // device geometry
     ExactTables ex;                  // EXACT family
+    ExactHostTables hx;              // host copies of ex
+    FwdSlabCfg fslab;                // slab forward projector (R == 0: not used)
     float *d_src = nullptr;          // RC family: [P][3] sources (float3 layout)
     float *d_org = nullptr;          // RC family: [P][3] detector origins
 
@@ -107,6 +129,7 @@ struct kv_plan {
     const void *graph_p = nullptr;
     const void *graph_x = nullptr;
     int graph_iters = 0, graph_mlem = 0, graph_fb = 0, graph_bb = 0;
+    long long graph_slab = 0;
     float graph_relax = 0.f;
 };
 
@@ -208,7 +231,7 @@ struct BackArgs {
 };
 
 kv_status exact_build_tables(kv_plan *plan, const float *src, const float *det, int n_views,
-                             ExactTables *out);
+                             ExactTables *out, ExactHostTables *host);
 void exact_free_tables(ExactTables *t);
 
 kv_status exact_forward_launch(kv_plan *plan, const ExactTables &t, int n_views, FwdMode mode,
@@ -236,6 +259,17 @@ kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_s
 kv_status convert_back_launch(kv_ctx *ctx, const void *in, float *out, size_t n, kv_storage s);
 kv_status phantom_launch(kv_ctx *ctx, int nx, int ny, int nz, float dx, float dy, float dz,
                          const float *d_params, int n, float *vol);
+
+// Slab-staged EXACT forward projector (kv_fwd_slab.cu).  fwd_slab_fit checks
+// that the plan's geometry suits it (at most three columns and five rows per
+// ray and slice, boxes within 256 voxels and the shared-memory budget) and
+// sizes its boxes for (R, S, stages, group); fwd_slab_launch runs it for
+// views [0, n_views) of the tables `t` (the plan's own, possibly offset).
+bool fwd_slab_fit(const kv_plan *plan, int R, int S, int stages, int group, FwdSlabCfg *out, std::string *why);
+int fwd_slab_default_group(int n_views);
+size_t fwd_slab_blocks(const kv_plan *plan, int n_views);
+kv_status fwd_slab_launch(kv_plan *plan, const ExactTables &t, int n_views, FwdMode mode, const FwdArgs &a,
+                          double *partials);
 
 // RC driver epilogue modes (forward: ratio / residual fused; back: update fused)
 enum RcMode : int { RC_PLAIN = 0, RC_MLEM = 1, RC_ART = 2 };

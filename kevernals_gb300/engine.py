@@ -336,6 +336,21 @@ def _plan_set_tuning(self, fwd_rows, back_rows):
     self.ctx.check(lib().kv_plan_set_tuning(self._h, int(fwd_rows), int(back_rows)))
 
 
+def _plan_slab(self):
+    """(rays per thread, slices per slab, stages, view group) of the slab
+    forward projector; rays per thread 0: the one-thread-per-ray kernel."""
+    v = [C.c_int() for _ in range(4)]
+    self.ctx.check(lib().kv_plan_get_slab(self._h, *(C.byref(x) for x in v)))
+    return tuple(x.value for x in v)
+
+
+def _plan_set_slab(self, rays_per_thread, slices=4, stages=3, view_group=16):
+    self.ctx.check(lib().kv_plan_set_slab(self._h, int(rays_per_thread), int(slices), int(stages),
+                                          int(view_group)))
+
+
+Plan.slab = property(_plan_slab)
+Plan.set_slab = _plan_set_slab
 Plan.autotune = _plan_autotune
 Plan.tuning = property(_plan_tuning)
 Plan.set_tuning = _plan_set_tuning

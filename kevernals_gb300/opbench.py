@@ -52,6 +52,8 @@ def main(argv=None):
     ap.add_argument("--workload", default="chest4", choices=["chest", "chest4", "small", "column"])
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--slab", default="",
+                    help="forward projector shape: 'off' (one thread per ray) or R,S,stages,group")
     args = ap.parse_args(argv)
     import torch
 
@@ -87,6 +89,9 @@ def main(argv=None):
     def plan(family):
         if family not in plans:
             plans[family] = engine.Plan(ctx, g, family)
+            if family == "exact" and args.slab:
+                shape = [0] if args.slab == "off" else [int(v) for v in args.slab.split(",")]
+                plans[family].set_slab(*shape)
         return plans[family]
 
     p = plan("exact").forward(truth)

@@ -182,7 +182,7 @@ def test_host_entry_points_run_clean_under_sanitizers(lib, tmp_path):
                     "-fPIC,-fsanitize=address,-fsanitize=undefined,-fno-omit-frame-pointer",
                     "-I", os.path.join(root, "include"), "-I", csrc, "-c", os.path.join(csrc, "kv_api.cu"),
                     "-o", api], check=True, capture_output=True)
-    objs = [os.path.join(kb.BUILD, f"{s}.o") for s in ("kv_exact", "kv_rc", "kv_misc", "kv_unet")]
+    objs = [os.path.join(kb.BUILD, os.path.splitext(s)[0] + ".o") for s in kb.SOURCES if s != "kv_api.cu"]
     so = str(tmp_path / "libkvtomo_asan.so")
     subprocess.run([kb.nvcc(), "-shared", *kb.ARCH, "-o", so, api, *objs, "-lcudart", "-Xcompiler",
                     "-fsanitize=address,-fsanitize=undefined"], check=True, capture_output=True)

@@ -61,7 +61,12 @@ def test_graph_captured_loop_matches_stepwise(ctx):
 
 
 def test_batch_matches_one_by_one(ctx):
+    """The persistent batch (one-thread-per-ray forward tiles) against each
+    plan's own solve (the slab forward projector where the geometry suits
+    it: the same weights, summed in another order) and against the FP64
+    oracle's MLEM."""
     import torch
+    from oracle import oracle as O
     cases = batch_cases(6, 321, scale=4)
     plans = [engine.Plan(ctx, g, "exact") for g in cases]
     data = [make_data(ctx, g, 100 + i) for i, g in enumerate(cases)]
@@ -71,7 +76,12 @@ def test_batch_matches_one_by_one(ctx):
         ref = torch.ones(plan.geometry.volume_shape, device="cuda")
         plan.mlem(p, ref, 5)
         torch.cuda.synchronize()
-        assert torch.equal(x, ref)
+        assert float((x - ref).norm() / ref.norm()) < 1e-5
+    smallest = sorted(zip(cases, data, xs), key=lambda c: c[0].n_voxels + c[0].n_rays)[:2]
+    for g, p, x in smallest:                            # the two smallest cases against FP64
+        xo = O.exact_mlem(g, p.cpu().numpy().astype(np.float64), np.ones(g.volume_shape), 5)
+        xg = x.cpu().numpy()
+        assert np.linalg.norm(xg - xo) / np.linalg.norm(xo) < 1e-5
     # host buffers through the same entry point
     hp = [p.cpu().numpy() for p in data]
     hx = [np.ones(g.volume_shape, np.float32) for g in cases]
@@ -106,7 +116,7 @@ def test_batch_throughput_vs_one_by_one(ctx):
           f"({rays / t_batch:.3e} rays/s), one by one {t_seq:.3f} s ({rays / t_seq:.3e} rays/s), "
           f"speed-up {t_seq / t_batch:.2f}x")
     for x, y in zip(xs, ys):
-        assert torch.equal(x, y)
+        assert float((x - y).norm() / y.norm()) < 1e-4
 
 
 def test_autotune_picks_valid_shapes(ctx):

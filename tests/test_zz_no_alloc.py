@@ -61,3 +61,37 @@ def test_noalloc_residual_rejects_oversize_geometry():
     status, _, _ = _noalloc(plan, dummy, dummy)
     assert status == 1                                  # KV_ERR_INVALID_ARG
     assert "static scratch" in ctx.last_error()
+
+
+def test_noalloc_residual_block_limit_is_exact():
+    """At exactly KV_NOALLOC_MAX_BLOCKS forward blocks the call is accepted
+    and matches kv_residual; one block more is refused.  Blocks are
+    ceil(nu / 32) * ceil(nv / fwd_rows) * n_views with the plan's forward
+    block height, set here to one row."""
+    torch = pytest.importorskip("torch")
+    from kevernals_gb300 import build, engine
+    from kevernals_gb300.geometry import linear_sweep
+
+    build.build()
+    max_blocks = 65536
+    ctx = engine.Context(0)
+    # 1 column tile x 1024 rows x 64 views = 65536 blocks of 32 x 1 rays
+    g = linear_sweep(32, 32, 8, 0.5, 0.5, 1.0, 64, 32, 1024, 0.4, 0.0125, 15.0)
+    plan = engine.Plan(ctx, g, "exact")
+    plan.set_tuning(1, 8)
+    assert ((g.nu + 31) // 32) * g.nv * g.n_views == max_blocks
+    x = torch.rand(g.volume_shape, device="cuda") + 0.5
+    p = plan.forward(x) * 1.01
+    for call in range(2):
+        want_r, want_ll = plan.residual(p, x)
+        status, r, ll = _noalloc(plan, p, x)
+        assert status == 0, ctx.last_error()
+        assert r == pytest.approx(want_r, rel=TOL) and ll == pytest.approx(want_ll, rel=TOL)
+        x.mul_(1.1)
+    # one block more: 65537 rows of one view
+    g2 = linear_sweep(32, 32, 8, 0.5, 0.5, 1.0, 1, 32, max_blocks + 1, 0.4, 0.0002, 15.0)
+    plan2 = engine.Plan(ctx, g2, "exact")
+    plan2.set_tuning(1, 8)
+    dummy = torch.zeros(4, device="cuda")
+    status, _, _ = _noalloc(plan2, dummy, dummy)
+    assert status == 1 and "static scratch" in ctx.last_error()
