@@ -15,13 +15,16 @@ ratio, backprojection with the fused multiplicative update).
   roofline   the dominant kernel's algorithmic bytes per launch over its
              live average duration (per-launch CUDA events), against the
              measured HBM copy bandwidth.
-  cpu_baseline  the oracle (FP64 Siddon, all host cores) on a bounded sample
-             of rays of the same workload, extrapolated to the metric.
+  cpu_baseline  the reference's CPU MLEM iteration (as --impl reference) on
+             a bounded sample of the same workload, all host cores.
 
 --impl reference times the reference's own CPU path for the same metric:
-its MLEM iteration (reference-compatible forward with the reference's
-selection sort, windowed backprojector, host ratio/update loops, as restated
-in oracle/) on sampled rays and voxels of the same workload, all host cores.
+its MLEM iteration (forward projection with the reference's selection sort,
+11x11-window backprojection, the serial host ratio and update loops) on the
+host cores -- the reference's Projector.cu kernels compiled for the host
+where they were built (oracle/_ref), else their restatement in oracle/ --
+whole iterations at the small workload, a bounded sample of rays and voxels
+per step at chest-DT; rate = work done / measured step time.
 
 Multi-GPU (torchrun): replicas only -- each rank solves its own seeded case;
 value = all ranks' rays / max-over-ranks time.
@@ -57,6 +60,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=None,
+                    help="reference arm: size each step's sample to about this many seconds "
+                         "(default: whole iterations at the small workload, 5 s at chest-DT)")
     ap.add_argument("--no-ttr", action="store_true",
                     help="skip the learned-warm-start time-to-residual comparison")
     ap.add_argument("--no-ref-gpu", action="store_true",
@@ -160,78 +166,101 @@ def algorithmic_bytes(kernel, g, sv, sp):
 
 # ---------------------------------------------------------------- the arms
 
-def cpu_baseline_exact(g, truth_np, p_np, seconds, seed=0):
-    """FP64 oracle forward + transpose on a bounded sample of rays, all
-    host cores; extrapolated to rays/s of the MLEM iteration."""
+def reference_cpu_steps(g, truth, steps, warmup, seconds=None, fraction=None, seed=1):
+    """The reference's MLEM iteration (Reconstructors.h:182-242: forward
+    projection, host ratio loop, backprojection, host update loop) on the
+    host cores, each step on a bounded sample: a fraction f of the rays and
+    the same fraction of the voxels.  The kernels are the reference's own
+    Projector.cu compiled for the host (oracle/_ref, all cores) where the
+    reference tree was present at build time, else their restatement in the
+    oracle (the reference's selection sort and 11x11-window backprojector);
+    the host loops are the reference's serial loops restated.  f = 1 runs
+    whole iterations; otherwise f is sized so that a step takes about
+    `seconds`.  Returns (step times, units of work per step, description,
+    kind, cores, the iterate after the last step)."""
     from oracle import oracle as O
+    use_ref = O.ref_lib() is not None
     rng = np.random.default_rng(seed)
-    vol64 = truth_np.astype(np.float64)
-    back = np.zeros(g.volume_shape, np.float64)
-    n = 2000
-    while True:
-        rays = rng.integers(0, g.n_rays, n)
+    x = np.ones(g.volume_shape, np.float32)          # the uniform start
+    p = np.zeros(g.proj_shape, np.float32)           # measurements at the sampled rays
+    q = np.zeros(g.proj_shape, np.float32)           # forward projection, then ratio
+    b = np.zeros(g.volume_shape, np.float32)         # backprojection
+    relax = 1.0
+
+    def forward(vol, rays, out):
+        if use_ref:
+            O.ref_forward_rays(g, vol, rays, out)
+        else:
+            out.reshape(-1)[rays] = O.rc_forward_rays_refcost(g, vol, rays)
+
+    def back(proj, vox, out):
+        if use_ref:
+            O.ref_back_voxels(g, proj, vox, out)
+        else:
+            out.reshape(-1)[vox] = O.rc_back_voxels(g, proj, vox)
+
+    def sample(f):
+        if f >= 1.0:
+            return np.arange(g.n_rays, dtype=np.int64), np.arange(g.n_voxels, dtype=np.int64)
+        nr, nv = max(1, int(round(f * g.n_rays))), max(1, int(round(f * g.n_voxels)))
+        return (np.unique(rng.integers(0, g.n_rays, nr)), np.unique(rng.integers(0, g.n_voxels, nv)))
+
+    def step(rays, vox):
         t0 = time.perf_counter()
-        O.exact_forward_rays(g, vol64, rays)
-        t1 = time.perf_counter()
-        O.exact_back_rays(g, p_np.reshape(-1)[rays].astype(np.float64), rays, back)
-        t2 = time.perf_counter()
-        if t2 - t0 > 0.25 * seconds or n >= 1 << 22:
-            break
-        n = int(n * min(16.0, max(2.0, 0.3 * seconds / max(t2 - t0, 1e-3))))
-    rate = 2 * n / (t2 - t0)
-    return {"value": rate, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-            "sample": f"{n} random rays of the workload: FP64 Siddon forward ({t1 - t0:.2f} s) and "
-                      f"transpose ({t2 - t1:.2f} s); rate = 2 * rays / time"}
+        forward(x, rays, q)
+        O.rc_mlem_host_loops(p, q, rays, x, b, vox[:0], relax)       # ratio loop
+        back(q, vox, b)
+        O.rc_mlem_host_loops(p, q, rays[:0], x, b, vox, relax)       # update loop
+        return time.perf_counter() - t0
+
+    if fraction is None:
+        fraction = 1.0
+        if seconds is not None:
+            f0 = min(1.0, 4096.0 / g.n_rays)
+            rays, vox = sample(f0)
+            forward(truth, rays, p)
+            t = step(rays, vox)
+            fraction = min(1.0, f0 * seconds / max(t, 1e-4))
+    rays, vox = sample(fraction)
+    forward(truth, rays, p)                          # the sampled rays' measurements
+    for _ in range(warmup):
+        step(rays, vox)
+    times = [step(rays, vox) for _ in range(steps)]
+    units = len(rays) + len(vox) * g.n_rays / g.n_voxels     # rays, and voxels in ray units
+    what = ("the reference's Projector.cu kernels compiled for the host (OpenMP)" if use_ref
+            else "the oracle's restatement of the reference kernels (selection sort, 11x11 window; OpenMP)")
+    desc = (f"{'whole iterations' if fraction >= 1.0 else f'{len(rays)} random rays and {len(vox)} random voxels per step (fraction {fraction:.3g} of an iteration)'}"
+            f" of the reference's MLEM: {what}, with its serial host ratio and update loops; "
+            f"rate = (rays + voxels x P*D/V) per step / step time")
+    return times, units, desc, ("reference" if use_ref else "port"), O.num_threads(), x
 
 
 def reference_arm(args, g, desc):
-    """The reference's MLEM iteration on the host cores, sampled."""
+    """The reference's MLEM iteration on the host cores (reference_cpu_steps)."""
     from kevernals_gb300 import phantom as ph
     from oracle import oracle as O
     _, n_ell, i0, cfg, _ = geometry(args.workload)
     params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, n_ell, ph.seed_for(cfg))
     truth = O.phantom(g, params)
-    rng = np.random.default_rng(1)
-    proj = np.zeros(g.proj_shape, np.float32)
-    nr, nv = 256, 256
-
-    def one_step():
-        rays = rng.integers(0, g.n_rays, nr)
-        vox = rng.integers(0, g.n_voxels, nv)
-        t0 = time.perf_counter()
-        O.rc_forward_rays_refcost(g, truth, rays)
-        t1 = time.perf_counter()
-        O.rc_back_voxels(g, proj, vox)
-        t2 = time.perf_counter()
-        # full iteration time: all rays, all voxels, plus the host ratio and update loops
-        t_iter = (t1 - t0) * g.n_rays / nr + (t2 - t1) * g.n_voxels / nv
-        return t_iter, t2 - t0
-
-    # size the samples to about two seconds of host work per step
-    for _ in range(3):
-        t_iter, wall = one_step()
-        if wall > 1.0:
-            break
-        nr, nv = nr * 4, nv * 4
-    iters = []
-    for _ in range(args.warmup):
-        one_step()
-    for _ in range(args.steps):
-        iters.append(one_step()[0])
-    t_iter = statistics.mean(iters)
-    value = 2 * g.n_rays / t_iter
-    cores = O.num_threads()
-    sample = (f"per step {nr} random rays (forward, reference selection sort) and {nv} random voxels "
-              f"(11x11-window backprojector) of the workload, extrapolated to one MLEM iteration "
-              f"({t_iter:.1f} s)")
+    seconds = args.ref_seconds if args.ref_seconds is not None else (None if args.workload == "small" else 5.0)
+    times, units, sample, kind, cores, _ = reference_cpu_steps(g, truth, args.steps, args.warmup, seconds=seconds)
+    t = statistics.mean(times)
+    value = units / t
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded ellipsoid phantom", "config": {"workload": desc, "family": "rc",
-                                                                       "step": "one MLEM iteration"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+                                                                       "step": sample, "rays_per_step": units},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(g, truth_np, seconds):
+    """The reference's CPU MLEM iteration on a bounded sample of the same
+    workload (about `seconds` of host work), rays/s."""
+    times, units, sample, kind, cores, _ = reference_cpu_steps(g, truth_np, 1, 0, seconds=seconds)
+    return {"value": units / times[0], "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
 
 
 def reference_gpu(g, truth):
@@ -442,7 +471,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
         ttr = time_to_residual(ctx, g, cfg, rank)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline_exact(g, truth.cpu().numpy(), p.cpu().numpy(), args.cpu_seconds)
+        cpu = cpu_baseline(g, truth.cpu().numpy(), args.cpu_seconds)
     ref_gpu_line = reference_gpu(g, truth) if rank == 0 and not args.no_ref_gpu else None
 
     if rank == 0:

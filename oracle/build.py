@@ -22,7 +22,10 @@ REF_SO = os.path.join(HERE, "_ref", "libkvref.so")
 REF_GEOMETRY = os.path.join(HERE, "_ref", "ref_geometry")
 REF_HISTOGRAM = os.path.join(HERE, "_ref", "ref_histogram")
 REF_DRIVERS = os.path.join(HERE, "_ref", "ref_drivers")
-REFERENCE_ROOT = "/root/reference"
+# The reference tree: $KVTOMO_REFERENCE_ROOT, else a directory named
+# "reference" beside the one that holds this repository.
+REFERENCE_ROOT = (os.environ.get("KVTOMO_REFERENCE_ROOT")
+                  or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def build_oracle(force=False):

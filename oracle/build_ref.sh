@@ -33,13 +33,17 @@
 # for the engine's RC kernels, the "reference GPU" timing line, and the
 # checker for the drop-in's XML geometry reader.
 #
-# Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference-root>   (oracle/build.py passes it)
 # The kernel lines are extracted into oracle/_ref/ only for the compile and
 # removed afterwards; only the shared library stays.  Exits 0 without building
 # when the reference tree is absent.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+if [ $# -lt 1 ]; then
+    echo "usage: $0 <reference-root>" >&2
+    exit 2
+fi
+ref="$1"
 src="$ref/source/modules/reconstruction/Projector.cu"
 out="$here/_ref"
 if [ ! -f "$src" ]; then

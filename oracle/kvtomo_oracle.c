@@ -364,6 +364,22 @@ static int almost_equal_relative(float a, float b) {
     return diff <= scaled;
 }
 
+/* The host loops of one recons::MLEM iteration on a sample of indices, as
+ * the reference runs them (serial): the ratio q <- relax * p / q where
+ * q != 0 (Reconstructors.h:207-213) over the sampled rays, and the update
+ * x <- x * b (Reconstructors.h:238-241) over the sampled voxels. */
+void kvo_rc_mlem_host_loops(const float *p, float *q, const int64_t *rays, int64_t n_rays, float *x,
+                            const float *b, const int64_t *voxels, int64_t n_vox, float relax) {
+    for (int64_t i = 0; i < n_rays; ++i) {
+        const int64_t r = rays[i];
+        if (!almost_equal_relative(q[r], 0.F)) q[r] = relax * (p[r] / q[r]);
+    }
+    for (int64_t i = 0; i < n_vox; ++i) {
+        const int64_t j = voxels[i];
+        x[j] *= b[j];
+    }
+}
+
 /* recons::MLEM, Reconstructors.h:182-242; x updated in place. */
 void kvo_rc_mlem(const kvo_geom *g, const float *p, float *x, int iters, float relax) {
     size_t np = (size_t)g->nu * g->nv * g->n_views, nvox = (size_t)g->nx * g->ny * g->nz;

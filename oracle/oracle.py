@@ -71,6 +71,8 @@ def lib():
             "kvo_exact_sart": [G, _f64p, _f64p, C.c_int, C.c_double],
             "kvo_phantom": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                             _f32p, C.c_int, _f32p],
+            "kvo_rc_mlem_host_loops": [_f32p, _f32p, _i64p, C.c_int64, _f32p, _f32p, _i64p, C.c_int64,
+                                       C.c_float],
             "kvo_num_threads": [],
             "kvo_set_threads": [C.c_int],
         }
@@ -96,6 +98,10 @@ def ref_lib():
         L.kvref_back.argtypes = [G, _f32p, _f32p]
         L.kvref_forward.restype = None
         L.kvref_back.restype = None
+        L.kvref_forward_rays.argtypes = [G, _f32p, _i64p, C.c_int64, _f32p]
+        L.kvref_back_voxels.argtypes = [G, _f32p, _i64p, C.c_int64, _f32p]
+        L.kvref_forward_rays.restype = None
+        L.kvref_back_voxels.restype = None
         _ref = L
     return _ref
 
@@ -255,6 +261,41 @@ def ref_back(g, proj):
     out = np.empty(g.volume_shape, np.float32)
     L.kvref_back(C.byref(cgeom(g)), _proj(g, proj, np.float32), out)
     return out
+
+
+def ref_forward_rays(g, vol, rays, proj):
+    """The reference's forward kernel on sampled rays, written into the
+    full projection stack `proj` (float32, in place)."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference kernels not built (reference tree absent)")
+    rays = np.ascontiguousarray(rays, np.int64)
+    assert proj.dtype == np.float32 and proj.flags.c_contiguous and proj.size == g.n_rays
+    L.kvref_forward_rays(C.byref(cgeom(g)), _vol(g, vol, np.float32), rays, rays.shape[0], proj)
+    return proj
+
+
+def ref_back_voxels(g, proj, voxels, vol):
+    """The reference's backprojection kernel on sampled voxels, written into
+    the full volume `vol` (float32, in place)."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference kernels not built (reference tree absent)")
+    voxels = np.ascontiguousarray(voxels, np.int64)
+    assert vol.dtype == np.float32 and vol.flags.c_contiguous and vol.size == g.n_voxels
+    L.kvref_back_voxels(C.byref(cgeom(g)), _proj(g, proj, np.float32), voxels, voxels.shape[0], vol)
+    return vol
+
+
+def rc_mlem_host_loops(p, q, rays, x, b, voxels, relax):
+    """The reference MLEM iteration's serial host loops on sampled indices
+    (ratio over rays, multiplicative update over voxels), in place."""
+    for a in (p, q, x, b):
+        assert a.dtype == np.float32 and a.flags.c_contiguous
+    rays = np.ascontiguousarray(rays, np.int64)
+    voxels = np.ascontiguousarray(voxels, np.int64)
+    lib().kvo_rc_mlem_host_loops(p.reshape(-1), q.reshape(-1), rays, rays.shape[0], x.reshape(-1),
+                                 b.reshape(-1), voxels, voxels.shape[0], float(relax))
 
 
 def ramp_taps(half_taps):

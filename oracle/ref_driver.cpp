@@ -109,3 +109,47 @@ extern "C" void kvref_back(const Geom *g, const float *proj, float *vol) {
         CudaPerformBackProjection(proj, vdim, vorg, vsp, vol, pdim, psp, org.data(), src.data());
     }
 }
+
+/* The reference's kernels on a sample: rays (indices into the projection
+ * stack) and voxels (indices into the volume), written into full-size
+ * buffers at those indices.  Used to time the reference's own CPU path on a
+ * bounded sample of a large workload. */
+extern "C" void kvref_forward_rays(const Geom *g, const float *vol, const int64_t *rays, int64_t n, float *proj) {
+    std::vector<float3> org, src;
+    views(*g, org, src);
+    dim3 vdim(g->nx, g->ny, g->nz), pdim(g->nu, g->nv, g->n_views);
+    float3 vorg{0.F, 0.F, 0.F}, vsp{g->dx, g->dy, g->dz};
+    float2 psp{g->du, g->dv};
+    const long long per_view = (long long)g->nu * g->nv;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+        const long long r = rays[i];
+        int view = (int)(r / per_view);
+        int v = (int)((r % per_view) / g->nu), u = (int)(r % g->nu);
+        if (!ray_hits(*g, view, u, v)) {
+            proj[r] = 0.F;
+            continue;
+        }
+        blockDim = dim3(1, 1, 1);
+        threadIdx = dim3(0, 0, 0);
+        blockIdx = dim3(u, v, view);
+        CudaPerformProjection(vol, vdim, vorg, vsp, proj, pdim, psp, org.data(), src.data());
+    }
+}
+
+extern "C" void kvref_back_voxels(const Geom *g, const float *proj, const int64_t *voxels, int64_t n, float *vol) {
+    std::vector<float3> org, src;
+    views(*g, org, src);
+    dim3 vdim(g->nx, g->ny, g->nz), pdim(g->nu, g->nv, g->n_views);
+    float3 vorg{0.F, 0.F, 0.F}, vsp{g->dx, g->dy, g->dz};
+    float2 psp{g->du, g->dv};
+    const long long plane = (long long)g->nx * g->ny;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+        const long long w = voxels[i];
+        blockDim = dim3(1, 1, 1);
+        threadIdx = dim3(0, 0, 0);
+        blockIdx = dim3((unsigned)(w % g->nx), (unsigned)((w % plane) / g->nx), (unsigned)(w / plane));
+        CudaPerformBackProjection(proj, vdim, vorg, vsp, vol, pdim, psp, org.data(), src.data());
+    }
+}

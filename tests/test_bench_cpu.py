@@ -20,3 +20,20 @@ def test_gather_rate_counts_siddon_segments():
     assert bench.gather_rate("exact_back", g, 2, 2, 10.0)["gather_bytes"] == 2 * seg
     assert bench.gather_rate("rc_back", g, 4, 4, 10.0) == {}
     assert "gather_unavailable" in bench.gather_rate("exact_fwd", None, 4, 4, 10.0)
+
+
+def test_reference_cpu_step_is_one_reference_mlem_iteration():
+    """With the whole workload as its sample, a step of the timed reference
+    arm is one iteration of the reference's MLEM (forward, ratio loop,
+    backprojection, update loop) from the uniform start, bit for bit."""
+    import numpy as np
+    from kevernals_gb300 import phantom as ph
+    from kevernals_gb300.geometry import linear_sweep
+    from oracle import oracle as O
+    g = linear_sweep(24, 20, 6, 0.5, 0.5, 1.0, 5, 24, 20, 0.4, 0.4, 10.0)
+    truth = O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 5, 7))
+    times, units, desc, kind, cores, x = bench.reference_cpu_steps(g, truth, 1, 0, fraction=1.0)
+    p = O.rc_forward(g, truth)
+    want = O.rc_mlem(g, p, np.ones(g.volume_shape, np.float32), 1, 1.0)
+    assert np.array_equal(x, want)
+    assert units == 2 * g.n_rays and len(times) == 1 and "whole iterations" in desc

@@ -55,7 +55,7 @@ def test_max_over_ranks_gloo_world2():
 def test_reference_arm_runs_on_rank0_only_under_torchrun():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
-           "--impl", "reference", "--gpus", "2", "--workload", "small", "--steps", "1", "--warmup", "0"]
+           "--impl", "reference", "--gpus", "2", "--workload", "small", "--steps", "1", "--warmup", "0", "--ref-seconds", "1"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
