@@ -229,6 +229,17 @@ kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_rows);
 kv_status kv_plan_get_slab(const kv_plan *plan, int *rays_per_thread, int *slices, int *stages, int *view_group);
 kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int slices, int stages, int view_group);
 
+/* Work per thread of the EXACT gather backprojector (no reference
+ * counterpart; it replaces the per-voxel-thread CudaPerformBackProjection,
+ * Projector.cu:376-785, on the EXACT path): voxel rows per thread share each
+ * thread's candidate-column intervals, and consecutive slices per thread
+ * are summed view by view so that they reuse each view's detector patch
+ * from cache.  Shapes (rows, slices): (1, 1), (2, 1), (2, 2); rows 0 selects
+ * one voxel per thread in blocks of 32 x back_rows of kv_plan_set_tuning.
+ * Default (2, 2). */
+kv_status kv_plan_get_back_shape(const kv_plan *plan, int *rows_per_thread, int *slices_per_thread);
+kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_per_thread);
+
 /* ---- learned warm start (no reference counterpart) ----------------------
  * A 3D U-Net (4 levels, 16/32/64/128 channels, 3x3x3 convolutions, BF16
  * weights and activations, FP32 accumulation, tensor-core implicit-GEMM

@@ -70,6 +70,8 @@ SIGNATURES = {
     "kv_plan_get_slab": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                           C.POINTER(C.c_int)], C.c_int),
     "kv_plan_set_slab": ([_vp, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
+    "kv_plan_get_back_shape": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+    "kv_plan_set_back_shape": ([_vp, C.c_int, C.c_int], C.c_int),
     "kv_unet_create": ([_vp, C.c_uint64, C.POINTER(_vp)], C.c_int),
     "kv_unet_destroy": ([_vp], C.c_int),
     "kv_unet_num_params": ([_vp], C.c_size_t),

@@ -735,7 +735,8 @@ kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float 
     const bool same = plan->graph_exec != nullptr && plan->graph_p == p && plan->graph_x == x &&
                       plan->graph_iters == iters && plan->graph_mlem == (int)mlem && plan->graph_relax == relax &&
                       plan->graph_fb == plan->fwd_by && plan->graph_bb == plan->back_by &&
-                      plan->graph_slab == slab_key(plan->fslab);
+                      plan->graph_slab == slab_key(plan->fslab) && plan->graph_br == plan->back_rows &&
+                      plan->graph_bs == plan->back_slices;
     if (!same) {
         if (plan->graph_exec != nullptr) {
             KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -768,6 +769,8 @@ kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float 
         plan->graph_fb = plan->fwd_by;
         plan->graph_bb = plan->back_by;
         plan->graph_slab = slab_key(plan->fslab);
+        plan->graph_br = plan->back_rows;
+        plan->graph_bs = plan->back_slices;
     }
     KV_CHECK_CUDA(ctx, cudaGraphLaunch(plan->graph_exec, ctx->stream));
     return KV_OK;
@@ -1031,5 +1034,25 @@ extern "C" kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int sl
         return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "slab shape (%d, %d, %d, %d) does not fit: %s",
                        rays_per_thread, slices, stages, view_group, why.c_str());
     plan->fslab = c;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_get_back_shape(const kv_plan *plan, int *rows_per_thread, int *slices_per_thread) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (rows_per_thread) *rows_per_thread = plan->back_rows;
+    if (slices_per_thread) *slices_per_thread = plan->back_slices;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_per_thread) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    const bool ok = rows_per_thread == 0 || (rows_per_thread == 1 && slices_per_thread == 1) ||
+                    (rows_per_thread == 2 && (slices_per_thread == 1 || slices_per_thread == 2));
+    if (!ok)
+        return kv_fail(plan->ctx, KV_ERR_INVALID_ARG,
+                       "gather backprojector shape must be rows 0, (1, 1), (2, 1) or (2, 2)");
+    if (rows_per_thread == 0) slices_per_thread = 1;
+    plan->back_rows = rows_per_thread;
+    plan->back_slices = slices_per_thread;
     return KV_OK;
 }

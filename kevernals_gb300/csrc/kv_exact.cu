@@ -435,6 +435,182 @@ __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T
     back_tile<VolT, ProjT, ACC, MODE>(G, T, a, sens_out, blockIdx.x, blockIdx.y, z0 + (int)blockIdx.z);
 }
 
+// ---------------------------------------------------------------------------
+// Gather backprojector, R voxel rows and S slices per thread.  Block = 32 x 8
+// threads over 32 voxel columns (lanes) by 8R voxel rows (warp w owns rows
+// w, w + 8, ...) and S consecutive slices; views are the outer loop, so the
+// S slices read nearly the same detector patch of a view while it sits in
+// L1.  For each (view, slice) a lane computes the x-intervals of its voxel
+// column's candidate detector columns once -- only as many slots as the
+// warp's widest voxel needs -- and uses them for its R voxel rows; the
+// candidate detector rows of each voxel row go to shared memory as
+// t-intervals, one lane per candidate; the R voxel rows then run through
+// their candidate rows in lockstep (independent accumulators, so their loads
+// and sums overlap).  Weights are the same float expressions as back_tile's,
+// bit for bit.
+// ---------------------------------------------------------------------------
+
+// The terms of one chunk of NS candidate columns (ub .. ub + NS - 1) for the
+// R voxels of this thread, candidate rows c < nvc of the current row chunk.
+template <int NS, int R, typename ProjT, int ACC>
+__device__ __forceinline__ void back_chunk_r(const ExGeom &G, const ExactTables &T, int p, float htop, int i,
+                                             int ub, int u1, const ProjT *const (&rowp)[R], int nvc,
+                                             const float2 (*ys)[32], float *acc, float *comp) {
+    float lox[NS], hix[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        lox[s] = 1.f;
+        hix[s] = 0.f;
+        const int u = ub + s;
+        if (u <= u1) {
+            const float4 X = T.xt[(size_t)p * G.nu + u];
+            const int ib = T.xi[(size_t)p * G.nu + u];
+            const float ftx = __fmaf_rn(X.y, htop, X.x);
+            const float ta = cross_t(i - ib, ftx, X.z), tb = cross_t(i + 1 - ib, ftx, X.z);
+            lox[s] = fmaxf(0.f, fminf(ta, tb));
+            hix[s] = fminf(1.f, fmaxf(ta, tb));
+        }
+    }
+    for (int c = 0; c < nvc; ++c) {
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const float2 yi = ys[q][c];
+            const ProjT *row = rowp[q] + (size_t)c * G.nu;
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                const float w = __fsub_rn(fminf(hix[s], yi.y), fmaxf(lox[s], yi.x));
+                if (w > 0.f) back_accumulate<ACC>(w, Store<ProjT>::ld(row + s), acc[q], comp[q]);
+            }
+        }
+    }
+}
+
+template <typename VolT, typename ProjT, int ACC, int MODE, int R, int S>
+__device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &T, const BackArgs &a,
+                                            double *sens_out, int bx, int by, int k0, int kend) {
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int i = bx * 32 + lane;
+    const int jw = by * 8 * R + warp;          // voxel row of q = 0; rows jw + 8q
+    __shared__ float2 ysh[8][R][32];
+    const bool live_i = i < G.nx;
+    const ProjT *yp = static_cast<const ProjT *>(a.yp);
+    float acc[S][R], comp[S][R];
+#pragma unroll
+    for (int kk = 0; kk < S; ++kk)
+#pragma unroll
+        for (int q = 0; q < R; ++q) acc[kk][q] = comp[kk][q] = 0.f;
+    for (int p = 0; p < G.n_views; ++p) {
+#pragma unroll
+        for (int kk = 0; kk < S; ++kk) {
+            const int k = k0 + kk;
+            if (k >= kend) break;   // block-uniform
+            const float htop = T.hr[(size_t)p * (G.nz + 1) + k + 1];
+            const float4 r0 = T.rng[(size_t)p * (G.nz + 1) + k];
+            const float4 r1 = T.rng[(size_t)p * (G.nz + 1) + k + 1];
+            // candidate detector columns of voxel column i (per lane)
+            const float ulo = fminf(((float)i - r0.x) * r0.y, ((float)i - r1.x) * r1.y);
+            const float uhi = fmaxf(((float)(i + 1) - r0.x) * r0.y, ((float)(i + 1) - r1.x) * r1.y);
+            const int u0 = max(0, (int)ceilf(fminf(ulo, uhi) - 0.01f));
+            int u1 = min(G.nu - 1, (int)floorf(fmaxf(ulo, uhi) + 0.01f));
+            if (!live_i) u1 = u0 - 1;
+            const int n_u_warp = __reduce_max_sync(0xffffffffu, u1 >= u0 ? u1 - u0 + 1 : 0);
+            // candidate detector rows of each voxel row (warp-uniform)
+            int v0[R], nvr[R], nvmax = 0;
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                const int j = jw + 8 * q;
+                nvr[q] = 0;
+                v0[q] = 0;
+                if (j < G.ny) {
+                    const float vlo = fminf(((float)j - r0.z) * r0.w, ((float)j - r1.z) * r1.w);
+                    const float vhi = fmaxf(((float)(j + 1) - r0.z) * r0.w, ((float)(j + 1) - r1.z) * r1.w);
+                    v0[q] = max(0, (int)ceilf(fminf(vlo, vhi) - 0.01f));
+                    const int v1 = min(G.nv - 1, (int)floorf(fmaxf(vlo, vhi) + 0.01f));
+                    nvr[q] = max(0, v1 - v0[q] + 1);
+                }
+                nvmax = max(nvmax, nvr[q]);
+            }
+            for (int vb = 0; vb < nvmax; vb += 32) {
+                // the rows' candidate intervals, one lane per candidate; entries past
+                // a row's candidates are empty (lo > hi) and weigh nothing
+#pragma unroll
+                for (int q = 0; q < R; ++q) {
+                    float2 iv = make_float2(1.f, 0.f);
+                    const int c = vb + lane;
+                    if (c < nvr[q]) {
+                        const int vv = v0[q] + c, j = jw + 8 * q;
+                        const float4 Y = T.yt[(size_t)p * G.nv + vv];
+                        const int jb = T.yi[(size_t)p * G.nv + vv];
+                        const float fty = __fmaf_rn(Y.y, htop, Y.x);
+                        const float ta = cross_t(j - jb, fty, Y.z), tb = cross_t(j + 1 - jb, fty, Y.z);
+                        iv = make_float2(fmaxf(0.f, fminf(ta, tb)), fminf(1.f, fmaxf(ta, tb)));
+                    }
+                    ysh[warp][q][lane] = iv;
+                }
+                __syncwarp();
+                const int nvc = min(32, nvmax - vb);
+                for (int cb = 0; cb * BACK_SLOTS < n_u_warp; ++cb) {
+                    const int ub = u0 + cb * BACK_SLOTS;
+                    const int nslot = min(BACK_SLOTS, n_u_warp - cb * BACK_SLOTS);
+                    const ProjT *rowp[R];
+#pragma unroll
+                    for (int q = 0; q < R; ++q) rowp[q] = yp + ((size_t)p * G.nv + v0[q] + vb) * G.nu + ub;
+                    float *ak = acc[kk], *ck = comp[kk];
+                    // nslot is warp-uniform: one unrolled chunk per slot count
+                    switch (nslot) {
+                    case 1: back_chunk_r<1, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 2: back_chunk_r<2, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 3: back_chunk_r<3, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 4: back_chunk_r<4, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 5: back_chunk_r<5, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 6: back_chunk_r<6, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    case 7: back_chunk_r<7, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    default: back_chunk_r<8, R, ProjT, ACC>(G, T, p, htop, i, ub, u1, rowp, nvc, ysh[warp], ak, ck); break;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (!live_i) return;
+#pragma unroll
+    for (int kk = 0; kk < S; ++kk) {
+        const int k = k0 + kk;
+        if (k >= kend) break;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const int j = jw + 8 * q;
+            if (j >= G.ny) continue;
+            const size_t idx = ((size_t)k * G.ny + j) * G.nx + i;
+            if (sens_out != nullptr) {
+                sens_out[idx] = ACC == ACC_DF ? (double)acc[kk][q] + (double)comp[kk][q] : (double)acc[kk][q];
+                continue;
+            }
+            VolT *vol = static_cast<VolT *>(a.vol);
+            const float b = (float)acc[kk][q];
+            if (MODE == BACK_PLAIN) {
+                Store<VolT>::st(vol + idx, b);
+            } else if (MODE == BACK_MLEM) {
+                const double sv = a.sens[idx];
+                if (sv > 0.0)
+                    Store<VolT>::st(vol + idx, (float)((double)Store<VolT>::ld_rw(vol + idx) * (double)b / sv));
+            } else if (MODE == BACK_SART) {
+                const double sv = a.sens[idx];
+                if (sv > 0.0)
+                    Store<VolT>::st(vol + idx, Store<VolT>::ld_rw(vol + idx) + (float)((double)(a.relax * b) / sv));
+            }
+        }
+    }
+}
+
+// Slices z0 .. z0 + nzs - 1, S per block.
+template <typename VolT, typename ProjT, int ACC, int MODE, int R, int S>
+__global__ void __launch_bounds__(256) exact_back_r_kernel(ExGeom G, ExactTables T, BackArgs a,
+                                                           double *sens_out, int z0, int nzs) {
+    back_tile_r<VolT, ProjT, ACC, MODE, R, S>(G, T, a, sens_out, blockIdx.x, blockIdx.y, z0 + S * (int)blockIdx.z,
+                                              z0 + nzs);
+}
+
 ExGeom exgeom(const kv_plan *plan, int n_views) {
     return ExGeom{plan->g.nx, plan->g.ny, plan->g.nz, plan->g.nu, plan->g.nv, n_views};
 }
@@ -557,9 +733,36 @@ kv_status fwd_dispatch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
     return KV_OK;
 }
 
+template <typename VolT, typename ProjT, int ACC, int R, int S>
+void back_r_launch(const ExGeom &G, const ExactTables &t, BackMode mode, const BackArgs &a, double *sens_out,
+                   int z0, int nzs, cudaStream_t st) {
+    dim3 block(32, 8), grid((G.nx + 31) / 32, (G.ny + 8 * R - 1) / (8 * R), (nzs + S - 1) / S);
+    switch (mode) {
+    case BACK_PLAIN: exact_back_r_kernel<VolT, ProjT, ACC, BACK_PLAIN, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
+    case BACK_MLEM: exact_back_r_kernel<VolT, ProjT, ACC, BACK_MLEM, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
+    case BACK_SART: exact_back_r_kernel<VolT, ProjT, ACC, BACK_SART, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
+    }
+}
+
+// (rows per thread, slices per thread): (1, 1), (2, 1) or (2, 2)
+template <typename VolT, typename ProjT, int ACC>
+void back_r_dispatch(int R, int S, const ExGeom &G, const ExactTables &t, BackMode mode, const BackArgs &a,
+                     double *sens_out, int z0, int nzs, cudaStream_t st) {
+    if (R == 1) back_r_launch<VolT, ProjT, ACC, 1, 1>(G, t, mode, a, sens_out, z0, nzs, st);
+    else if (S == 1) back_r_launch<VolT, ProjT, ACC, 2, 1>(G, t, mode, a, sens_out, z0, nzs, st);
+    else back_r_launch<VolT, ProjT, ACC, 2, 2>(G, t, mode, a, sens_out, z0, nzs, st);
+}
+
 template <typename VolT, typename ProjT>
 kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan, int z0, int nzs) {
     ExGeom G = exgeom(plan, plan->g.n_views);
+    if (plan->back_rows > 0) {
+        LaunchTimer lt(plan->ctx, "exact_back");
+        if (kahan) back_r_dispatch<VolT, ProjT, ACC_KAHAN>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
+        else back_r_dispatch<VolT, ProjT, ACC_F32>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
+        KV_CHECK_LAUNCH(plan->ctx, "exact_back_r_kernel");
+        return KV_OK;
+    }
     dim3 block(32, plan->back_by);
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, nzs);
     cudaStream_t st = plan->ctx->stream;
@@ -681,7 +884,10 @@ kv_status exact_sensitivity_launch(kv_plan *plan, double *sens) {
     dim3 grid((G.nx + 31) / 32, (G.ny + plan->back_by - 1) / plan->back_by, G.nz);
     {
         LaunchTimer lt(plan->ctx, "exact_back_sens_f64");
-        exact_back_kernel<float, float, ACC_DF, BACK_PLAIN><<<grid, block, 0, st>>>(G, plan->ex, a, sens, 0);
+        if (plan->back_rows > 0)
+            back_r_dispatch<float, float, ACC_DF>(plan->back_rows, plan->back_slices, G, plan->ex, BACK_PLAIN, a, sens, 0, G.nz, st);
+        else
+            exact_back_kernel<float, float, ACC_DF, BACK_PLAIN><<<grid, block, 0, st>>>(G, plan->ex, a, sens, 0);
     }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(ls, st);

@@ -121,7 +121,9 @@ struct kv_plan {
 
     // launch tuning (set by kv_plan_autotune or defaults)
     int fwd_by = 4;                  // forward block = 32 x fwd_by rays
-    int back_by = 8;                 // backprojector block = 32 x back_by voxels
+    int back_by = 8;                 // backprojector block = 32 x back_by voxels (one voxel per thread)
+    int back_rows = 2;               // voxel rows per thread of the gather backprojector (0: one voxel per thread)
+    int back_slices = 2;             // slices per thread of the gather backprojector
 
     // captured iteration loop (kv_mlem / kv_sart without callback), reused
     // while the buffers and parameters are the same
@@ -130,6 +132,7 @@ struct kv_plan {
     const void *graph_x = nullptr;
     int graph_iters = 0, graph_mlem = 0, graph_fb = 0, graph_bb = 0;
     long long graph_slab = 0;
+    int graph_br = 0, graph_bs = 0;
     float graph_relax = 0.f;
 };
 

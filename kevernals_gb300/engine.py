@@ -349,6 +349,20 @@ def _plan_set_slab(self, rays_per_thread, slices=4, stages=3, view_group=16):
                                           int(view_group)))
 
 
+def _plan_back_shape(self):
+    """(voxel rows, slices) per thread of the gather backprojector (rows 0:
+    one voxel per thread)."""
+    r, z = C.c_int(), C.c_int()
+    self.ctx.check(lib().kv_plan_get_back_shape(self._h, C.byref(r), C.byref(z)))
+    return r.value, z.value
+
+
+def _plan_set_back_shape(self, rows_per_thread, slices_per_thread=1):
+    self.ctx.check(lib().kv_plan_set_back_shape(self._h, int(rows_per_thread), int(slices_per_thread)))
+
+
+Plan.back_shape = property(_plan_back_shape)
+Plan.set_back_shape = _plan_set_back_shape
 Plan.slab = property(_plan_slab)
 Plan.set_slab = _plan_set_slab
 Plan.autotune = _plan_autotune

@@ -52,6 +52,8 @@ def main(argv=None):
     ap.add_argument("--workload", default="chest4", choices=["chest", "chest4", "small", "column"])
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--back-shape", default="",
+                    help="gather backprojector: rows,slices per thread (rows 0: one voxel per thread)")
     ap.add_argument("--slab", default="",
                     help="forward projector shape: 'off' (one thread per ray) or R,S,stages,group")
     args = ap.parse_args(argv)
@@ -92,6 +94,8 @@ def main(argv=None):
             if family == "exact" and args.slab:
                 shape = [0] if args.slab == "off" else [int(v) for v in args.slab.split(",")]
                 plans[family].set_slab(*shape)
+            if family == "exact" and args.back_shape:
+                plans[family].set_back_shape(*[int(v) for v in args.back_shape.split(",")])
         return plans[family]
 
     p = plan("exact").forward(truth)

@@ -360,3 +360,68 @@ def chord_lengths(g, rays):
     lo = np.maximum(0.0, np.minimum(t0, t1).max(axis=1))
     hi = np.minimum(1.0, np.maximum(t0, t1).min(axis=1))
     return np.maximum(hi - lo, 0.0) * np.linalg.norm(d, axis=1)
+
+
+# ---------------------------------------------------------------- kernel shapes
+
+def test_forward_slab_shapes_agree_and_match_fp64(ctx):
+    """Every slab shape of the forward projector (rays per thread, slices per
+    slab, stages, view group) sums each ray in the same order, so all give
+    the same projections bit for bit; the one-thread-per-ray kernel sums the
+    same weights in another order.  Both against the FP64 oracle."""
+    for g in small_geoms():
+        vol = phantom_for(g)
+        ref = O.exact_forward(g, vol.astype(np.float64))
+        plan = engine.Plan(ctx, g, "exact")
+        if (g.nx * 4) % 16 != 0:
+            # the volume's rows are no whole number of 16-byte TMA units: the
+            # plan keeps the one-thread-per-ray kernel and refuses slab shapes
+            assert plan.slab[0] == 0
+            with pytest.raises(KvError):
+                plan.set_slab(4, 4, 3, 16)
+            assert rel_l2(plan.forward(vol), ref) < EXACT_FWD_REL_L2
+            plan.close()
+            continue
+        assert plan.slab[0] > 0                              # the default path is the slab kernel
+        outs = []
+        for shape in [(8, 4, 2, 16), (4, 4, 3, 16), (4, 2, 2, 2), (2, 8, 2, 1), (2, 1, 4, 3)]:
+            plan.set_slab(*shape)
+            assert plan.slab == shape[:3] + (min(shape[3], g.n_views),)
+            outs.append(plan.forward(vol))
+        for o in outs[1:]:
+            assert np.array_equal(o, outs[0])
+        assert rel_l2(outs[0], ref) < EXACT_FWD_REL_L2
+        plan.set_slab(0)
+        assert plan.slab[0] == 0
+        per_ray = plan.forward(vol)
+        assert rel_l2(per_ray, ref) < EXACT_FWD_REL_L2
+        assert rel_l2(outs[0], per_ray) < 1e-6
+        plan.close()
+
+
+def test_back_shapes_bit_identical(ctx):
+    """The gather backprojector's work shapes (voxel rows and slices per
+    thread, or one voxel per thread) evaluate the same weights in the same
+    order per voxel: identical volumes, and the FP64 oracle within tolerance;
+    likewise the FP64 sensitivity image."""
+    for g in small_geoms():
+        y = np.random.default_rng(3).random(g.proj_shape, dtype=np.float32)
+        ref = O.exact_back(g, y.astype(np.float64))
+        plan = engine.Plan(ctx, g, "exact")
+        assert plan.back_shape == (2, 2)
+        outs, sens = [], []
+        for shape in [(0, 1), (1, 1), (2, 1), (2, 2)]:
+            plan.set_back_shape(*shape)
+            outs.append(plan.back(y))
+            plan2 = engine.Plan(ctx, g, "exact")
+            plan2.set_back_shape(*shape)
+            sens.append(plan2.sensitivity())
+            plan2.close()
+        for o in outs[1:]:
+            assert np.array_equal(o, outs[0])
+        for s in sens[1:]:
+            assert np.array_equal(s, sens[0])
+        assert rel_l2(outs[0], ref) < EXACT_BACK_REL_L2
+        with pytest.raises(KvError):
+            plan.set_back_shape(1, 2)
+        plan.close()
