@@ -65,6 +65,8 @@ def parse():
                          "(default: whole iterations at the small workload, 5 s at chest-DT)")
     ap.add_argument("--no-ttr", action="store_true",
                     help="skip the learned-warm-start time-to-residual comparison")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the accuracy check and the SAA / SART / RC / storage runs")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip timing the reference's own CUDA kernels on a sample")
     ap.add_argument("--views", type=int, default=0,
@@ -355,6 +357,106 @@ def gather_rate(kernel, g, sv, sp, avg_ms):
         return {"gather_unavailable": f"{type(e).__name__}: {e}"}
 
 
+def cuda_ms(fn, reps=3, warmup=1):
+    """Median wall time of fn() in ms, CUDA events on the current stream."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return sorted(ts)[len(ts) // 2]
+
+
+def accuracy_vs_fp64(g, plan, truth, n_rays=4096, seed=7):
+    """The stated error of the benchmarked EXACT pair against the FP64
+    oracle on the bench's own phantom: the GPU forward projection on a
+    seeded sample of rays against the oracle's FP64 Siddon line integrals,
+    and the GPU backprojection of a projection stack that is zero except on
+    those rays (seeded float32 values) against the oracle's FP64 transpose
+    of the same rays, over the whole volume."""
+    import torch
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    rays = np.unique(rng.integers(0, g.n_rays, n_rays))
+    idx = torch.from_numpy(rays).to(truth.device)
+    fwd = plan.forward(truth)
+    got = fwd.reshape(-1)[idx].double().cpu().numpy()
+    del fwd
+    ref = O.exact_forward_rays(g, truth.double().cpu().numpy(), rays)
+    vals = rng.random(len(rays)).astype(np.float32)
+    y = torch.zeros(g.proj_shape, dtype=torch.float32, device=truth.device)
+    y.view(-1)[idx] = torch.from_numpy(vals).to(truth.device)
+    b = plan.back(y).double().cpu().numpy()
+    del y
+    ref_b = np.zeros(g.volume_shape, np.float64)
+    O.exact_back_rays(g, vals.astype(np.float64), rays, ref_b)
+    nz = ref_b != 0
+    return {"forward": {"rays": int(len(rays)), "rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                        "max_abs": float(np.abs(got - ref).max()),
+                        "max_rel_to_max": float(np.abs(got - ref).max() / np.abs(ref).max())},
+            "back": {"rays": int(len(rays)), "voxels_touched": int(nz.sum()),
+                     "rel_l2": float(np.linalg.norm(b - ref_b) / np.linalg.norm(ref_b)),
+                     "max_abs": float(np.abs(b - ref_b).max()),
+                     "max_rel_to_max": float(np.abs(b - ref_b).max() / np.abs(ref_b).max())},
+            "oracle": "FP64 Siddon (oracle/kvtomo_oracle.c), tolerance 2e-6 relative L2 (tests)"}
+
+
+def config2_runs(ctx, g, plan, p, peak):
+    """The rest of the chest-DT run set beside the MLEM step: shift-and-add,
+    20 SART iterations at relaxation 0.5, the reference-compatible (RC)
+    family's MLEM iteration (the reference's own operator, like-for-like
+    with the reference arm), and BF16 / FP16 storage against FP32."""
+    import torch
+    from kevernals_gb300 import engine
+    out = {}
+    # shift-and-add (detector-sized slices, Reconstructors.h:263-379)
+    saa = plan.shift_and_add(p)
+    ms = cuda_ms(lambda: plan.shift_and_add(p, out=saa))
+    byts = 4 * (g.n_rays + g.nu * g.nv * g.nz)
+    out["shift_and_add"] = {"ms": ms, "algorithmic_bytes": byts, "GB/s": byts / (ms * 1e-3) / 1e9,
+                            "frac_hbm": byts / (ms * 1e-3) / 1e9 / peak,
+                            "parity": "shift rule equal to the reference's own code; zero padding and the 1/P "
+                                      "weighted sum restated (VTK absent): parity unpinned at that boundary"}
+    del saa
+    # 20 SART iterations, relaxation 0.5, from zero (graph-captured loop)
+    x = torch.zeros(g.volume_shape, dtype=torch.float32, device=p.device)
+    plan.sart(p, x, 20, 0.5)                     # capture + sensitivity, untimed
+    x.zero_()
+    ms = cuda_ms(lambda: plan.sart(p, x.zero_(), 20, 0.5), reps=1, warmup=0)
+    res, _ = plan.residual(p, x)
+    out["sart_20"] = {"iterations": 20, "relax": 0.5, "ms": ms, "ms_per_iteration": ms / 20,
+                      "rays_per_s": 2 * g.n_rays * 20 / (ms * 1e-3), "rel_residual": res}
+    del x
+    # RC family: the reference's operator on this GPU
+    rc = engine.Plan(ctx, g, "rc")
+    xr = torch.ones(g.volume_shape, dtype=torch.float32, device=p.device)
+    ms = cuda_ms(lambda: rc.mlem(p, xr, 1), reps=2, warmup=1)
+    out["rc_mlem_iteration"] = {"ms": ms, "rays_per_s": 2 * g.n_rays / (ms * 1e-3), "family": "rc",
+                                "note": "reference-compatible operator (bit-identical to the reference's kernels)"}
+    rc.close()
+    del xr
+    # storage precision: iteration time against FP32 (5 iterations per call)
+    times = {}
+    for storage in ("f32", "bf16", "f16"):
+        ps = engine.Plan(ctx, g, "exact", storage)
+        xs = torch.ones(g.volume_shape, dtype=torch.float32, device=p.device)
+        ms = cuda_ms(lambda: ps.mlem(p, xs, 5), reps=2, warmup=1)
+        times[storage] = ms / 5
+        ps.close()
+        del xs
+    out["storage_mlem_ms_per_iteration"] = times
+    out["storage_speedup_vs_f32"] = {k: times["f32"] / v for k, v in times.items() if k != "f32"}
+    return out
+
+
 def max_over_ranks(ms, world, device):
     """The slowest rank's time: replicas finish when the last one does.  One
     all-reduce (MAX) over the process group; the identity on one rank."""
@@ -461,6 +563,11 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
                "h2d_bytes_per_step": 4 * (g.n_rays + g.n_voxels), "d2h_bytes_per_step": 4 * g.n_voxels,
                "ms_per_step": ems / args.steps}
 
+    acc = extra = None
+    if not args.no_extras and args.family == "exact" and args.storage == "f32":
+        acc = accuracy_vs_fp64(g, plan, truth)
+        extra = config2_runs(ctx, g, plan, p, measured_hbm()[0])
+
     # the learned-warm-start comparison runs before the CPU and reference
     # legs, on a GPU and host that nothing else is using
     ttr = None
@@ -486,6 +593,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": gpu_launches, "roofline": roof,
             "cpu_baseline": cpu, "reference_gpu": ref_gpu_line, "time_to_residual": ttr,
+            "accuracy_vs_fp64": acc, "chest_runs": extra,
             "kernels": {k: {"launches": n, "avg_ms": t / n} for k, (n, t) in kernels.items()},
         }
         print(json.dumps(out), flush=True)

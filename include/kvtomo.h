@@ -208,10 +208,15 @@ kv_status kv_batch_mlem(kv_ctx *ctx, int n, kv_plan *const *plans, const float *
                         float *const *volumes, int iterations, float relax, kv_mem mem);
 
 /* Autotuner (no reference counterpart; the reference launches every kernel
- * with a fixed 32x16 block).  Times the EXACT forward projector with ray
- * bundles of 32 x {1,2,4,8} and the backprojector with voxel tiles of
- * 32 x {2,4,8} on (a subset of the views of) this plan's geometry and keeps
- * the fastest; results are cached per geometry shape for the process. */
+ * with a fixed 32x16 block).  On (a subset of the views of) this plan's
+ * geometry it times the slab forward projector's shapes (rays per thread,
+ * slices per slab, stages: see kv_plan_set_slab), the gather
+ * backprojector's shapes (kv_plan_set_back_shape, including one voxel per
+ * thread) and the one-thread-per-ray / per-voxel kernels' block heights
+ * (32 x {1,2,4,8} rays, 32 x {2,4,8} voxels), each the median of three
+ * timed runs, and keeps the fastest; results are cached per geometry shape
+ * and storage for the process.  kv_plan_get_tuning reports the block
+ * heights. */
 kv_status kv_plan_autotune(kv_plan *plan);
 kv_status kv_plan_get_tuning(const kv_plan *plan, int *fwd_rows, int *back_rows);
 kv_status kv_plan_set_tuning(kv_plan *plan, int fwd_rows, int back_rows);

@@ -656,7 +656,7 @@ extern "C" kv_status kv_shift_and_add(kv_plan *plan, const float *proj, float *s
     KV_TRY(stage_in(plan, proj, mem, &plan->d_proj32, plan->nproj, true, &pd));
     if (mem == KV_MEM_DEVICE) od = slices;
     else KV_CHECK_CUDA(plan->ctx, cudaMallocAsync((void **)&od, nout * sizeof(float), plan->ctx->stream));
-    kv_status s = saa_launch(plan, plan->d_shift, pd, od);
+    kv_status s = saa_launch(plan, plan->d_shift, sh.data(), pd, od);
     if (s == KV_OK && mem == KV_MEM_HOST) s = stage_out(plan, slices, mem, od, nout);
     if (mem == KV_MEM_HOST) cudaFreeAsync(od, plan->ctx->stream);
     return s;

@@ -603,11 +603,15 @@ __device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &
     }
 }
 
-// Slices z0 .. z0 + nzs - 1, S per block.
+// Slices z0 .. z0 + nzs - 1, S per block.  Grid (slice groups, voxel-row
+// tiles, voxel-column tiles): the slice group varies fastest, so the blocks
+// in flight cover a strip of voxel columns at every height, whose detector
+// footprint over all views stays in L2 while the strip's rows are swept
+// (slice groups slowest re-read every projection image once per group).
 template <typename VolT, typename ProjT, int ACC, int MODE, int R, int S>
 __global__ void __launch_bounds__(256) exact_back_r_kernel(ExGeom G, ExactTables T, BackArgs a,
                                                            double *sens_out, int z0, int nzs) {
-    back_tile_r<VolT, ProjT, ACC, MODE, R, S>(G, T, a, sens_out, blockIdx.x, blockIdx.y, z0 + S * (int)blockIdx.z,
+    back_tile_r<VolT, ProjT, ACC, MODE, R, S>(G, T, a, sens_out, blockIdx.z, blockIdx.y, z0 + S * (int)blockIdx.x,
                                               z0 + nzs);
 }
 
@@ -736,7 +740,7 @@ kv_status fwd_dispatch(kv_plan *plan, const ExactTables &t, int P, FwdMode mode,
 template <typename VolT, typename ProjT, int ACC, int R, int S>
 void back_r_launch(const ExGeom &G, const ExactTables &t, BackMode mode, const BackArgs &a, double *sens_out,
                    int z0, int nzs, cudaStream_t st) {
-    dim3 block(32, 8), grid((G.nx + 31) / 32, (G.ny + 8 * R - 1) / (8 * R), (nzs + S - 1) / S);
+    dim3 block(32, 8), grid((nzs + S - 1) / S, (G.ny + 8 * R - 1) / (8 * R), (G.nx + 31) / 32);
     switch (mode) {
     case BACK_PLAIN: exact_back_r_kernel<VolT, ProjT, ACC, BACK_PLAIN, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
     case BACK_MLEM: exact_back_r_kernel<VolT, ProjT, ACC, BACK_MLEM, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
@@ -1183,8 +1187,88 @@ void tune(kv_ctx *ctx, const ExGeom &G, const ExactTables &T, void *vol, void *p
     cudaEventDestroy(e1);
 }
 
+// Median of three timed calls of fn after one untimed call, in ms.
+template <typename F>
+float median3(kv_ctx *ctx, cudaEvent_t e0, cudaEvent_t e1, F fn) {
+    fn();
+    float t[3];
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0, ctx->stream);
+        fn();
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&t[r], e0, e1);
+    }
+    std::sort(t, t + 3);
+    return t[1];
+}
+
+// The shapes the tuner picked for one geometry shape and storage.
+struct TuneResult {
+    int fwd_by, back_by;
+    FwdSlabCfg fslab;
+    int back_rows, back_slices;
+};
+
 std::mutex g_tune_mutex;
-std::vector<std::pair<std::vector<long long>, std::pair<int, int>>> g_tune_cache;
+std::vector<std::pair<std::vector<long long>, TuneResult>> g_tune_cache;
+
+// The slab forward shapes and gather backprojector shapes, timed through the
+// plan's own launchers on its first (at most) 12 views.
+template <typename VolT, typename ProjT, int ACC>
+kv_status tune_shapes(kv_plan *plan, int P, TuneResult &best) {
+    kv_ctx *ctx = plan->ctx;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const kv_geometry &g = plan->g;
+    float bt = 1e30f;
+    static const int shapes[][3] = {{8, 4, 2}, {4, 4, 3}, {8, 2, 2}, {4, 2, 3}, {2, 4, 3}};
+    const int group = fwd_slab_default_group(g.n_views);
+    const FwdSlabCfg keep = plan->fslab;
+    const FwdArgs fa{plan->d_vol, nullptr, plan->d_ratio, nullptr, 1.f};
+    for (const auto &sh : shapes) {
+        FwdSlabCfg c;
+        if (!fwd_slab_fit(plan, sh[0], sh[1], sh[2], group, &c, nullptr)) continue;
+        plan->fslab = c;
+        const float ms = median3(ctx, e0, e1, [&] { exact_forward_launch(plan, plan->ex, P, FWD_PLAIN, fa); });
+        if (ms < bt) {
+            bt = ms;
+            best.fslab = c;
+        }
+    }
+    plan->fslab = keep;
+    // gather backprojector: (rows, slices) per thread, or one voxel per thread
+    const ExGeom G = exgeom(plan, P);
+    const BackArgs ba{plan->d_ratio, plan->d_vol, nullptr, 1.f};
+    static const int bshapes[][2] = {{2, 2}, {2, 1}, {1, 1}};
+    bt = 1e30f;
+    for (const auto &sh : bshapes) {
+        const float ms = median3(ctx, e0, e1, [&] {
+            back_r_dispatch<VolT, ProjT, ACC>(sh[0], sh[1], G, plan->ex, BACK_PLAIN, ba, nullptr, 0, g.nz, ctx->stream);
+        });
+        if (ms < bt) {
+            bt = ms;
+            best.back_rows = sh[0];
+            best.back_slices = sh[1];
+        }
+    }
+    {
+        dim3 block(32, best.back_by), grid((G.nx + 31) / 32, (G.ny + best.back_by - 1) / best.back_by, g.nz);
+        const float ms = median3(ctx, e0, e1, [&] {
+            exact_back_kernel<VolT, ProjT, ACC, BACK_PLAIN><<<grid, block, 0, ctx->stream>>>(G, plan->ex, ba, nullptr, 0);
+        });
+        if (ms < bt) {
+            best.back_rows = 0;
+            best.back_slices = 1;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+    return KV_OK;
+}
 
 }  // namespace
 
@@ -1195,12 +1279,18 @@ kv_status exact_autotune(kv_plan *plan) {
     kv_ctx *ctx = plan->ctx;
     const kv_geometry &g = plan->g;
     const std::vector<long long> key = {g.nx, g.ny, g.nz, g.nu, g.nv, g.n_views, (long long)plan->storage};
+    auto apply = [plan](const TuneResult &r) {
+        plan->fwd_by = r.fwd_by;
+        plan->back_by = r.back_by;
+        plan->fslab = r.fslab;
+        plan->back_rows = r.back_rows;
+        plan->back_slices = r.back_slices;
+    };
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         for (const auto &e : g_tune_cache)
             if (e.first == key) {
-                plan->fwd_by = e.second.first;
-                plan->back_by = e.second.second;
+                apply(e.second);
                 return KV_OK;
             }
     }
@@ -1210,17 +1300,24 @@ kv_status exact_autotune(kv_plan *plan) {
     KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_vol, 0, plan->nvox * es, ctx->stream));
     KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_ratio, 0, plan->nproj * es, ctx->stream));
     const ExGeom G = exgeom(plan, g.n_views < 6 ? g.n_views : 6);
-    int fb = plan->fwd_by, bb = plan->back_by;
+    TuneResult r{plan->fwd_by, plan->back_by, plan->fslab, plan->back_rows, plan->back_slices};
+    // one-thread-per-ray / per-voxel block heights (the fallback kernels)
     switch (plan->storage) {
-    case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
-    case KV_STORAGE_F16: tune<__half, __half, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
-    default: tune<float, float, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, fb, bb); break;
+    case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
+    case KV_STORAGE_F16: tune<__half, __half, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
+    default: tune<float, float, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
-    plan->fwd_by = fb;
-    plan->back_by = bb;
+    // slab forward and gather backprojector shapes
+    const int P = g.n_views < 12 ? g.n_views : 12;
+    switch (plan->storage) {
+    case KV_STORAGE_BF16: KV_TRY((tune_shapes<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(plan, P, r))); break;
+    case KV_STORAGE_F16: KV_TRY((tune_shapes<__half, __half, ACC_KAHAN>(plan, P, r))); break;
+    default: KV_TRY((tune_shapes<float, float, ACC_F32>(plan, P, r))); break;
+    }
+    apply(r);
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache.emplace_back(key, std::make_pair(fb, bb));
+    g_tune_cache.emplace_back(key, r);
     return KV_OK;
 }

@@ -255,7 +255,8 @@ kv_status rc_back_launch(kv_plan *plan, int mode, const float *proj, float *vol)
 // slices [z0, z0 + nzs) only; per voxel the arithmetic of the whole launch
 kv_status rc_back_slab_launch(kv_plan *plan, int mode, const float *proj, float *vol, int z0, int nzs);
 
-kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out);
+// shift-and-add; h_shift: the host copy of the [nz][P] shift table in d_shift
+kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const int32_t *h_shift, const float *proj, float *out);
 kv_status ramp_filter_launch(kv_plan *plan, const float *in, float *out, int half_taps);
 kv_status fill_launch(kv_ctx *ctx, float *p, size_t n, float v);
 kv_status convert_launch(kv_ctx *ctx, const float *in, void *out, size_t n, kv_storage s);

@@ -1,6 +1,8 @@
 // kv_misc.cu -- shift-and-add, phantom rasteriser and elementwise kernels.
 #include "kv_internal.h"
+#include "kv_tma.cuh"
 
+#include <algorithm>
 #include <cmath>
 
 namespace {
@@ -40,6 +42,106 @@ __global__ void __launch_bounds__(256) saa_kernel(int nu, int nv, int nz, int P,
             }
         }
         out[((size_t)k * nv + v) * nu + u] = (float)(((double)hi + (double)lo) * w);
+    }
+}
+
+// The same sums with each view's rows staged in shared memory.  A block
+// covers 32 detector columns x kSaaRows rows x kSaaSlices slices; for every
+// view one thread loads, by TMA, the band of that view's rows the block's
+// shifted rows reach (kSaaRows + the largest spread of the block's shifts;
+// rows outside the detector read zeros, which is the reference's zero
+// padding) into a ring of shared-memory stages, and every thread adds its
+// kSaaRows / 8 x kSaaSlices outputs' rows from the band.  Views are added in
+// the same order with the same TwoSum as saa_kernel, and a row outside the
+// detector adds an exact zero, so the two kernels agree bit for bit.
+constexpr int kSaaRows = 32, kSaaSlices = 4, kSaaStages = 3;
+constexpr uint32_t kSaaWaitPolls = 1u << 22;
+
+__global__ void __launch_bounds__(256) saa_band_kernel(const __grid_constant__ CUtensorMap pmap, int nu, int nv,
+                                                       int nz, int P, const int32_t *__restrict__ shift,
+                                                       float *__restrict__ out, int nb, uint32_t stage_stride,
+                                                       int *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t full[kSaaStages];
+    __shared__ int bstart[kSaaStages];
+    unsigned char *base = smem + ((128u - (kvtma::smem_u32(smem) & 127u)) & 127u);
+    float *bands = reinterpret_cast<float *>(base);
+    int *sh = reinterpret_cast<int *>(base + kSaaStages * stage_stride);     // [kSaaSlices][P]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int u0 = blockIdx.x * 32, v0 = blockIdx.y * kSaaRows, k0 = blockIdx.z * kSaaSlices;
+    const int kn = min(kSaaSlices, nz - k0);
+    for (int t = threadIdx.x; t < kn * P; t += blockDim.x) sh[t] = shift[(size_t)k0 * P + t];
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kSaaStages; ++s) kvtma::mbar_init(&full[s], 1);
+        kvtma::fence_mbar_init();
+    }
+    __syncthreads();
+    const uint32_t band_bytes = 32u * (uint32_t)nb * 4u;
+    auto issue = [&](int i, int st) {
+        int tmin = sh[i];
+        for (int kk = 1; kk < kn; ++kk) tmin = min(tmin, sh[kk * P + i]);
+        const int bs = v0 + tmin;
+        bstart[st] = bs;
+        kvtma::fence_proxy_async_smem();
+        kvtma::mbar_arrive_expect_tx(&full[st], band_bytes);
+        kvtma::tma_load_3d(kvtma::smem_u32(base + (size_t)st * stage_stride), &pmap, &full[st], u0, bs, i);
+    };
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kSaaStages && i < P; ++i) issue(i, i);
+    __syncthreads();
+    float hi[kSaaRows / 8][kSaaSlices], lo[kSaaRows / 8][kSaaSlices];
+#pragma unroll
+    for (int m = 0; m < kSaaRows / 8; ++m)
+#pragma unroll
+        for (int kk = 0; kk < kSaaSlices; ++kk) hi[m][kk] = lo[m][kk] = 0.f;
+    int err = 0, i = 0;
+    for (; i < P; ++i) {
+        const int st = i % kSaaStages;
+        if (!kvtma::mbar_wait_bounded(&full[st], (uint32_t)(i / kSaaStages) & 1u, kSaaWaitPolls)) err |= 1;
+        if (err == 0) {
+            const float *band = bands + (size_t)st * (stage_stride / 4);
+            const int rel = v0 + warp - bstart[st];
+#pragma unroll
+            for (int kk = 0; kk < kSaaSlices; ++kk) {
+                if (kk >= kn) break;
+                const int r0 = rel + sh[kk * P + i];
+#pragma unroll
+                for (int m = 0; m < kSaaRows / 8; ++m) {
+                    const int r = r0 + 8 * m;
+                    if ((unsigned)r >= (unsigned)nb) {   // outside the band: never expected
+                        err |= 4;
+                        continue;
+                    }
+                    const float x = band[r * 32 + lane];
+                    const float sm = hi[m][kk] + x;                 // TwoSum(hi, x)
+                    const float bp = sm - hi[m][kk];
+                    const float e = (hi[m][kk] - (sm - bp)) + (x - bp);
+                    hi[m][kk] = sm;
+                    lo[m][kk] += e;
+                }
+            }
+        }
+        if (__syncthreads_or(err)) break;
+        if (threadIdx.x == 0 && i + kSaaStages < P) issue(i + kSaaStages, st);
+    }
+    if (i < P) {   // failed: record, let the loads in flight land, leave
+        if (err) atomicOr(status, err);
+        if (threadIdx.x == 0)
+            for (int j = i; j < min(P, i + kSaaStages); ++j)
+                kvtma::mbar_wait_bounded(&full[j % kSaaStages], (uint32_t)(j / kSaaStages) & 1u, kSaaWaitPolls);
+        return;
+    }
+    const int u = u0 + lane;
+    if (u >= nu) return;
+    const double w = 1.0 / (double)P;
+#pragma unroll
+    for (int kk = 0; kk < kSaaSlices; ++kk) {
+        if (kk >= kn) break;
+#pragma unroll
+        for (int m = 0; m < kSaaRows / 8; ++m) {
+            const int v = v0 + warp + 8 * m;
+            if (v < nv) out[((size_t)(k0 + kk) * nv + v) * nu + u] = (float)(((double)hi[m][kk] + (double)lo[m][kk]) * w);
+        }
     }
 }
 
@@ -215,15 +317,59 @@ kv_status ramp_filter_launch(kv_plan *plan, const float *in, float *out, int hal
     return KV_OK;
 }
 
-kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const float *proj, float *out) {
+namespace {
+
+// Rows of the band a block of the staged kernel needs: kSaaRows + the
+// largest spread of one block's shifts over its slices, for any view.
+int saa_band_rows(const kv_geometry &g, const int32_t *sh) {
+    int span = 0;
+    for (int k0 = 0; k0 < g.nz; k0 += kSaaSlices)
+        for (int i = 0; i < g.n_views; ++i) {
+            int lo = sh[(size_t)k0 * g.n_views + i], hi = lo;
+            for (int k = k0 + 1; k < std::min(g.nz, k0 + kSaaSlices); ++k) {
+                lo = std::min(lo, sh[(size_t)k * g.n_views + i]);
+                hi = std::max(hi, sh[(size_t)k * g.n_views + i]);
+            }
+            span = std::max(span, hi - lo);
+        }
+    return kSaaRows + span;
+}
+
+}  // namespace
+
+kv_status saa_launch(kv_plan *plan, const int32_t *d_shift, const int32_t *h_shift, const float *proj, float *out) {
     const kv_geometry &g = plan->g;
+    kv_ctx *ctx = plan->ctx;
+    // the staged kernel where its band fits and TMA can address the stack
+    const int nb = saa_band_rows(g, h_shift);
+    const uint32_t stride = (uint32_t)((32u * nb * 4u + 127u) / 128u * 128u);
+    const size_t smem = (size_t)kSaaStages * stride + (size_t)kSaaSlices * g.n_views * sizeof(int32_t) + 128;
+    if (nb <= 256 && smem <= 160 * 1024 && (g.nu * 4) % 16 == 0 && reinterpret_cast<uintptr_t>(proj) % 16 == 0 &&
+        kvtma::encoder() != nullptr) {
+        CUtensorMap map;
+        cuuint64_t dims[3] = {(cuuint64_t)g.nu, (cuuint64_t)g.nv, (cuuint64_t)g.n_views};
+        cuuint64_t strides[2] = {(cuuint64_t)g.nu * 4, (cuuint64_t)g.nu * g.nv * 4};
+        cuuint32_t box[3] = {32, (cuuint32_t)nb, 1};
+        cuuint32_t es[3] = {1, 1, 1};
+        if (kvtma::encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(proj), dims, strides, box,
+                             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+            KV_CHECK_CUDA(ctx, cudaFuncSetAttribute(saa_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            dim3 grid((g.nu + 31) / 32, (g.nv + kSaaRows - 1) / kSaaRows, (g.nz + kSaaSlices - 1) / kSaaSlices);
+            LaunchTimer lt(ctx, "saa");
+            saa_band_kernel<<<grid, 256, smem, ctx->stream>>>(map, g.nu, g.nv, g.nz, g.n_views, d_shift, out, nb,
+                                                              stride, ctx->d_status);
+            KV_CHECK_LAUNCH(ctx, "saa_band_kernel");
+            return KV_OK;
+        }
+    }
     const int kb = 8;
     dim3 block(32, 8), grid((g.nu + 31) / 32, (g.nv + 7) / 8, (g.nz + kb - 1) / kb);
-    size_t smem = (size_t)kb * g.n_views * sizeof(int32_t);
-    if (smem > 48 * 1024) return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "shift-and-add: too many views");
-    LaunchTimer lt(plan->ctx, "saa");
-    saa_kernel<<<grid, block, smem, plan->ctx->stream>>>(g.nu, g.nv, g.nz, g.n_views, d_shift, proj, out, kb);
-    KV_CHECK_LAUNCH(plan->ctx, "saa_kernel");
+    size_t smem1 = (size_t)kb * g.n_views * sizeof(int32_t);
+    if (smem1 > 48 * 1024) return kv_fail(ctx, KV_ERR_UNSUPPORTED, "shift-and-add: too many views");
+    LaunchTimer lt(ctx, "saa");
+    saa_kernel<<<grid, block, smem1, ctx->stream>>>(g.nu, g.nv, g.nz, g.n_views, d_shift, proj, out, kb);
+    KV_CHECK_LAUNCH(ctx, "saa_kernel");
     return KV_OK;
 }
 

@@ -110,6 +110,26 @@ def config_chest() -> Geometry:
     return linear_sweep(1024, 1024, 128, 0.4, 0.4, 2.5, 60, 2048, 2048, 0.2, 0.2, 17.5)
 
 
+def uneven_cases(n: int, seed: int, scale: int = 1):
+    """Seeded uneven reconstruction problems (the batched-solve workload):
+    in-plane 128-512 voxels (multiples of 32), 32-96 slices, detector
+    256-1024 square, 9-49 views over +-10..+-25 deg; 0.5x0.5x1.0 mm voxels,
+    0.4 mm pixels.  `scale` > 1 shrinks every size by that factor (many
+    small problems)."""
+    from .phantom import SplitMix64
+    rng = SplitMix64(seed)
+    out = []
+    for _ in range(n):
+        nxy = 32 * int(rng.uniform(4, 17))
+        nz = int(rng.uniform(32, 97))
+        nd = int(rng.uniform(256, 1025))
+        views = int(rng.uniform(9, 50))
+        ang = rng.uniform(10.0, 25.0)
+        out.append(linear_sweep(nxy // scale, nxy // scale, max(2, nz // scale), 0.5 * scale, 0.5 * scale,
+                                1.0 * scale, views, nd // scale, nd // scale, 0.4 * scale, 0.4 * scale, ang))
+    return out
+
+
 def scaled(g: Geometry, factor: int) -> Geometry:
     """Same physical acquisition with volume and detector sampled `factor`
     times coarser (used for quick checks of a large workload)."""

@@ -27,7 +27,7 @@ UNET_FLOP_PER_VOXEL = (sum(2 * 27 * cin * cout / 8 ** lvl for cin, cout, lvl in 
     (192, 64, 2), (64, 64, 2), (96, 32, 1), (32, 32, 1), (48, 16, 0), (16, 16, 0))) + 2 * 27 * 16 + 2 * 16)
 
 OPS = ["exact_fwd", "exact_back", "mlem_iter", "sart_iter", "rc_fwd", "rc_back", "saa",
-       "phantom", "unet_fwd", "unet_train"]
+       "phantom", "unet_fwd", "unet_train", "batch_small"]
 
 
 def _geometry(name):
@@ -149,6 +149,29 @@ def main(argv=None):
                 print(json.dumps({"op": op, "workload": args.workload, "ms": ms,
                                   "TFLOP/s": 3 * flop_fwd / (ms * 1e-3) / 1e12}), flush=True)
             net.close()
+        elif op == "batch_small":
+            # many small problems: 256 seeded uneven cases at a quarter of the
+            # batched workload's sizes, 30 MLEM iterations, one persistent
+            # launch per phase (kv_batch_mlem) against solving one by one
+            from .geometry import uneven_cases
+            cases = uneven_cases(256, 20261203 + 3000, scale=4)
+            bplans, data = [], []
+            for ci, gc in enumerate(cases):
+                pc = engine.Plan(ctx, gc, "exact")
+                tc = engine.phantom(ctx, gc, ph.ellipsoid_params(gc.nx, gc.ny, gc.nz, gc.dx, gc.dy, gc.dz, 20,
+                                                                   3000 + ci), device=True)
+                data.append(pc.forward(tc))
+                pc.sensitivity(device=True)
+                bplans.append(pc)
+            xs = [torch.ones(gc.volume_shape, device="cuda") for gc in cases]
+            t_batch = timed(lambda: [x.fill_(1.0) for x in xs] and engine.batch_mlem(ctx, bplans, data, xs, 30))
+            t_seq = timed(lambda: [pc.mlem(d, x.fill_(1.0), 30) for pc, d, x in zip(bplans, data, xs)])
+            rays = sum(2 * gc.n_rays for gc in cases) * 30
+            print(json.dumps({"op": op, "cases": len(cases), "iterations": 30, "batched_ms": t_batch,
+                              "one_by_one_ms": t_seq, "speedup": t_seq / t_batch,
+                              "batched_rays_per_s": rays / (t_batch * 1e-3)}), flush=True)
+            for pc in bplans:
+                pc.close()
         else:
             raise SystemExit(f"unknown op {op}")
     for pl in plans.values():

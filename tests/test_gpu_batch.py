@@ -7,26 +7,13 @@ import numpy as np
 import pytest
 
 from kevernals_gb300 import build, engine, phantom as ph
-from kevernals_gb300.geometry import linear_sweep
+from kevernals_gb300.geometry import linear_sweep, uneven_cases
 
 pytestmark = pytest.mark.gpu
 
 
 def batch_cases(n, seed, scale=1):
-    """Seeded uneven cases: in-plane 128-512 (multiples of 32), 32-96 slices,
-    detector 256-1024 square, 9-49 views over +-10..+-25 deg; 0.5x0.5x1.0 mm
-    voxels, 0.4 mm pixels.  `scale` > 1 shrinks every size for quick tests."""
-    rng = ph.SplitMix64(seed)
-    out = []
-    for _ in range(n):
-        nxy = 32 * int(rng.uniform(4, 17))
-        nz = int(rng.uniform(32, 97))
-        nd = int(rng.uniform(256, 1025))
-        views = int(rng.uniform(9, 50))
-        ang = rng.uniform(10.0, 25.0)
-        out.append(linear_sweep(nxy // scale, nxy // scale, max(2, nz // scale), 0.5 * scale, 0.5 * scale,
-                                1.0 * scale, views, nd // scale, nd // scale, 0.4 * scale, 0.4 * scale, ang))
-    return out
+    return uneven_cases(n, seed, scale)
 
 
 def make_data(ctx, g, seed):

@@ -233,6 +233,26 @@ def test_shift_and_add_vs_oracle(ctx, family, rule):
     assert np.abs(out - ref).max() <= 1e-6 * np.abs(ref).max()
 
 
+def test_shift_and_add_staged_equals_direct(ctx):
+    """The staged shift-and-add (TMA-loaded row bands; detector widths that
+    are whole 16-byte units) and the direct kernel (any width) add the same
+    rows in the same order: a detector widened by three columns, whose first
+    columns are the narrow one's, gives the narrow one's slices bit for bit;
+    both against the oracle, on geometries whose shifts leave the detector."""
+    for g in (small_geoms()[2], linear_sweep(48, 40, 9, 0.5, 0.5, 3.0, 11, 64, 56, 0.4, 0.4, 35.0)):
+        assert g.nu % 4 == 0
+        rng = np.random.default_rng(9)
+        p = rng.random(g.proj_shape, dtype=np.float32)
+        gw = Geometry(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, g.nu + 3, g.nv, g.du, g.dv, g.src, g.det_origin,
+                      g.fulcrum_z)
+        pw = np.concatenate([p, rng.random((g.n_views, g.nv, 3), dtype=np.float32)], axis=2)
+        staged = engine.Plan(ctx, g, "exact").shift_and_add(p)
+        direct = engine.Plan(ctx, gw, "exact").shift_and_add(pw)
+        assert np.array_equal(staged, direct[:, :, :g.nu])
+        ref = O.saa(g, p, 1)
+        assert np.abs(staged - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
 # ---------------------------------------------------------------- edges
 
 def test_device_buffers_match_host(ctx):
@@ -425,3 +445,23 @@ def test_back_shapes_bit_identical(ctx):
         with pytest.raises(KvError):
             plan.set_back_shape(1, 2)
         plan.close()
+
+
+def test_exact_config1_full_size_vs_fp64(ctx):
+    """The whole config-1 workload (256x256x64 voxels, 15 views of 512^2):
+    the forward projection of its seeded 40-ellipsoid phantom and the
+    backprojection of a seeded random projection stack against the FP64
+    oracle, every ray and every voxel."""
+    g = config_small()
+    vol = O.phantom(g, ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 40, ph.seed_for(1)))
+    plan = engine.Plan(ctx, g, "exact")
+    f = plan.forward(vol)
+    ref = O.exact_forward(g, vol.astype(np.float64))
+    assert rel_l2(f, ref) < EXACT_FWD_REL_L2
+    assert np.abs(f - ref).max() < 1e-5 * np.abs(ref).max()
+    y = np.random.default_rng(11).random(g.proj_shape, dtype=np.float32)
+    b = plan.back(y)
+    ref_b = O.exact_back(g, y.astype(np.float64))
+    assert rel_l2(b, ref_b) < EXACT_BACK_REL_L2
+    assert np.abs(b - ref_b).max() < 1e-5 * np.abs(ref_b).max()
+    plan.close()
