@@ -251,6 +251,38 @@ kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_
  * convolutions) mapping a shift-and-add volume [D][H][W] (float32) to an MLEM
  * initial estimate of the same size: y = x + f(x).  D and H must be multiples
  * of 8 and W of 128. */
+/* One of the network's convolutions on caller device buffers: out =
+ * conv3x3x3(in1 ++ in2, w) + bias, ReLU if relu != 0, zero padding.
+ * Channels-last BF16 (bit patterns) [D][H][W][C]: in1 has c1 channels, in2
+ * (may be NULL when c2 = 0) c2 channels concatenated after them, out cout
+ * channels; w is [cout][27][c1 + c2] BF16 (taps z, y, x), bias cout floats
+ * or NULL; FP32 accumulation.  kernel: 0 = tcgen05 / TMA implicit GEMM where
+ * the volume is a whole number of 128-voxel tiles, else mma.sync; 1 =
+ * tcgen05 only; 2 = mma.sync only.  Channel counts: multiples of 16 (the
+ * tcgen05 kernel: 16, 32, 64 or 128 per input, cout <= 256).  Stream-ordered
+ * on the context's stream; a tensor-core pipeline wait that gives up is
+ * reported by the next kv_sync. */
+kv_status kv_conv3_bf16(kv_ctx *ctx, const uint16_t *in1, int32_t c1, const uint16_t *in2, int32_t c2,
+                        const uint16_t *w, const float *bias, int32_t relu, uint16_t *out, int32_t cout,
+                        int32_t D, int32_t H, int32_t W, int32_t kernel);
+
+/* The learned warm start's elementwise steps on device buffers of n
+ * elements, on the context's stream (no reference counterpart).
+ *   kv_warm_ratio      ratio = a1 > 0 ? p / a1 : 0 -- the ray ratio of the
+ *                      volume-grid shift-and-add A^T(p / A1) / A^T 1 -- and,
+ *                      if uniform_residual is not NULL, ||a1 - p|| / ||p|| in
+ *                      FP64: the data residual of the uniform start, whose
+ *                      projection is the ray-length image a1 (synchronises).
+ *   kv_warm_normalize  out = sens > 0 ? b / sens : 0, divided in FP64.
+ *   kv_warm_fill       out = max(seen ? net : saa, eps): the network's
+ *                      estimate with the voxels no ray sees enough of taken
+ *                      from the shift-and-add volume, clamped positive. */
+kv_status kv_warm_ratio(kv_ctx *ctx, const float *p, const float *a1, float *ratio, size_t n,
+                        double *uniform_residual);
+kv_status kv_warm_normalize(kv_ctx *ctx, const float *b, const double *sens, float *out, size_t n);
+kv_status kv_warm_fill(kv_ctx *ctx, const float *net, const float *saa, const uint8_t *seen, float eps,
+                       float *out, size_t n);
+
 typedef struct kv_unet kv_unet;
 kv_status kv_unet_create(kv_ctx *ctx, uint64_t seed, kv_unet **out);
 kv_status kv_unet_destroy(kv_unet *net);

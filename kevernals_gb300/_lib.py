@@ -72,6 +72,11 @@ SIGNATURES = {
     "kv_plan_set_slab": ([_vp, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "kv_plan_get_back_shape": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "kv_plan_set_back_shape": ([_vp, C.c_int, C.c_int], C.c_int),
+    "kv_warm_ratio": ([_vp, _vp, _vp, _vp, C.c_size_t, C.POINTER(C.c_double)], C.c_int),
+    "kv_warm_normalize": ([_vp, _vp, _vp, _vp, C.c_size_t], C.c_int),
+    "kv_warm_fill": ([_vp, _vp, _vp, _vp, C.c_float, _vp, C.c_size_t], C.c_int),
+    "kv_conv3_bf16": ([_vp, _vp, C.c_int32, _vp, C.c_int32, _vp, _vp, C.c_int32, _vp, C.c_int32, C.c_int32,
+                       C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "kv_unet_create": ([_vp, C.c_uint64, C.POINTER(_vp)], C.c_int),
     "kv_unet_destroy": ([_vp], C.c_int),
     "kv_unet_num_params": ([_vp], C.c_size_t),

@@ -145,6 +145,81 @@ __global__ void __launch_bounds__(256) saa_band_kernel(const __grid_constant__ C
     }
 }
 
+// The learned warm start's elementwise steps.
+// ratio = a1 > 0 ? p / a1 : 0, and per block the FP64 sums of (a1 - p)^2 and
+// p^2 (the uniform start's data residual: its forward projection is a1).
+__global__ void __launch_bounds__(256) warm_ratio_kernel(const float *__restrict__ p, const float *__restrict__ a1,
+                                                         float *__restrict__ ratio, size_t n, double *partials) {
+    double d0 = 0.0, d1 = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float pv = p[i], av = a1[i];
+        ratio[i] = av > 0.f ? pv / av : 0.f;
+        const double d = (double)av - (double)pv;
+        d0 += d * d;
+        d1 += (double)pv * (double)pv;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+        d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+    }
+    __shared__ double red[2][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[0][warp] = d0;
+        red[1][warp] = d1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            s0 += red[0][w];
+            s1 += red[1][w];
+        }
+        partials[2 * blockIdx.x] = s0;
+        partials[2 * blockIdx.x + 1] = s1;
+    }
+}
+
+// out[0..1] = the sums of the per-block partial pairs (one block, fixed order)
+__global__ void sum_pairs_kernel(const double *partials, int nblocks, double *out) {
+    __shared__ double sh[2][256];
+    double s0 = 0.0, s1 = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        s0 += partials[2 * b];
+        s1 += partials[2 * b + 1];
+    }
+    sh[0][threadIdx.x] = s0;
+    sh[1][threadIdx.x] = s1;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0][0];
+        out[1] = sh[1][0];
+    }
+}
+
+// out = sens > 0 ? b / sens (in FP64, rounded once) : 0
+__global__ void warm_normalize_kernel(const float *__restrict__ b, const double *__restrict__ sens,
+                                      float *__restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double sv = sens[i];
+        out[i] = sv > 0.0 ? (float)((double)b[i] / sv) : 0.f;
+    }
+}
+
+// out = seen ? max(net, eps) : max(saa, eps)
+__global__ void warm_fill_kernel(const float *__restrict__ net, const float *__restrict__ saa,
+                                 const uint8_t *__restrict__ seen, float eps, float *__restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = fmaxf(seen[i] ? net[i] : saa[i], eps);
+}
+
 __global__ void fill_kernel(float *p, size_t n, float v) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         p[i] = v;
@@ -428,5 +503,58 @@ kv_status residual_reduce_launch(kv_ctx *ctx, const float *q, const float *p, si
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(partials, ctx->stream);
     if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "residual reduction: %s", cudaGetErrorString(e));
+    return KV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The learned warm start's elementwise steps (device buffers)
+// ---------------------------------------------------------------------------
+
+extern "C" kv_status kv_warm_ratio(kv_ctx *ctx, const float *p, const float *a1, float *ratio, size_t n,
+                                   double *uniform_residual) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (p == nullptr || a1 == nullptr || ratio == nullptr || n == 0)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_warm_ratio: null buffer or empty");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int blocks = grid_for(ctx, n, 256);
+    double *partials = nullptr;
+    KV_CHECK_CUDA(ctx, cudaMallocAsync((void **)&partials, 2 * sizeof(double) * blocks, ctx->stream));
+    {
+        LaunchTimer lt(ctx, "warm_ratio");
+        warm_ratio_kernel<<<blocks, 256, 0, ctx->stream>>>(p, a1, ratio, n, partials);
+        sum_pairs_kernel<<<1, 256, 0, ctx->stream>>>(partials, blocks, ctx->d_red);
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(partials, ctx->stream);
+    if (e != cudaSuccess) return kv_fail(ctx, KV_ERR_CUDA, "kv_warm_ratio: %s", cudaGetErrorString(e));
+    if (uniform_residual != nullptr) {
+        double h[2];
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_red, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+        KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        *uniform_residual = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
+    }
+    return KV_OK;
+}
+
+extern "C" kv_status kv_warm_normalize(kv_ctx *ctx, const float *b, const double *sens, float *out, size_t n) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (b == nullptr || sens == nullptr || out == nullptr || n == 0)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_warm_normalize: null buffer or empty");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    LaunchTimer lt(ctx, "warm_normalize");
+    warm_normalize_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(b, sens, out, n);
+    KV_CHECK_LAUNCH(ctx, "warm_normalize_kernel");
+    return KV_OK;
+}
+
+extern "C" kv_status kv_warm_fill(kv_ctx *ctx, const float *net, const float *saa, const uint8_t *seen, float eps,
+                                  float *out, size_t n) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (net == nullptr || saa == nullptr || seen == nullptr || out == nullptr || n == 0)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_warm_fill: null buffer or empty");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    LaunchTimer lt(ctx, "warm_fill");
+    warm_fill_kernel<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(net, saa, seen, eps, out, n);
+    KV_CHECK_LAUNCH(ctx, "warm_fill_kernel");
     return KV_OK;
 }

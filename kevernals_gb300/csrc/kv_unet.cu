@@ -821,3 +821,53 @@ extern "C" kv_status kv_unet_set_state(kv_unet *u, const float *state, int64_t s
     u->step = step;
     return KV_OK;
 }
+
+// One 3x3x3 convolution of the network's kind on caller buffers (device
+// pointers, BF16 bit patterns): the operator behind every U-Net layer, for
+// callers and tests that need a single layer.  kernel: 0 = the tensor-core
+// (tcgen05 / TMA) kernel where the volume tiles, else mma.sync; 1 = tcgen05
+// only; 2 = mma.sync only.
+extern "C" kv_status kv_conv3_bf16(kv_ctx *ctx, const uint16_t *in1, int32_t c1, const uint16_t *in2, int32_t c2,
+                                   const uint16_t *w, const float *bias, int32_t relu, uint16_t *out, int32_t cout,
+                                   int32_t D, int32_t H, int32_t W, int32_t kernel) {
+    if (ctx == nullptr) return KV_ERR_INVALID_ARG;
+    if (in1 == nullptr || w == nullptr || out == nullptr || (c2 > 0 && in2 == nullptr))
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_conv3_bf16: null buffer");
+    if (D <= 0 || H <= 0 || W <= 0 || c1 <= 0 || c2 < 0 || cout <= 0 || kernel < 0 || kernel > 2)
+        return kv_fail(ctx, KV_ERR_INVALID_ARG, "kv_conv3_bf16: bad sizes or kernel choice");
+    KV_CHECK_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bf16 *a = reinterpret_cast<const bf16 *>(in1), *b = reinterpret_cast<const bf16 *>(in2);
+    const bf16 *wb = reinterpret_cast<const bf16 *>(w);
+    bf16 *o = reinterpret_cast<bf16 *>(out);
+    int bw, bh, bd;
+    const bool tiles = convtc::tile_shape(D, H, W, bw, bh, bd);
+    if (kernel == 1 && !tiles)
+        return kv_fail(ctx, KV_ERR_UNSUPPORTED, "kv_conv3_bf16: the volume is not a whole number of 128-voxel tiles");
+    if (kernel != 2 && tiles) {
+        const char *why = convtc::launch(a, c1, c2 ? b : nullptr, c2, wb, bias, relu != 0, o, cout, D, H, W,
+                                         ctx->d_status, ctx->sm_count, ctx->stream);
+        if (why != nullptr) return kv_fail(ctx, KV_ERR_UNSUPPORTED, "tensor-core convolution: %s", why);
+        KV_CHECK_LAUNCH(ctx, "kv_conv3_bf16 (tcgen05)");
+        return KV_OK;
+    }
+    if (W % 16 != 0 || c1 % 16 != 0 || c2 % 16 != 0 || cout % 16 != 0)
+        return kv_fail(ctx, KV_ERR_UNSUPPORTED, "kv_conv3_bf16: mma.sync needs W, channels multiples of 16");
+    const long long nvox = (long long)D * H * W;
+    const int blocks = (int)((nvox / 16 + 3) / 4);
+    for (int n0 = 0; n0 < cout; n0 += 64) {
+        const int nc = cout - n0 < 64 ? cout - n0 : 64;
+        const bool rl = relu != 0;
+        switch (nc) {
+        case 16: rl ? unet::conv3_fwd<2, true><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W)
+                    : unet::conv3_fwd<2, false><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W); break;
+        case 32: rl ? unet::conv3_fwd<4, true><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W)
+                    : unet::conv3_fwd<4, false><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W); break;
+        case 48: rl ? unet::conv3_fwd<6, true><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W)
+                    : unet::conv3_fwd<6, false><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W); break;
+        default: rl ? unet::conv3_fwd<8, true><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W)
+                    : unet::conv3_fwd<8, false><<<blocks, 128, 0, ctx->stream>>>(a, c1, b, c2, wb, bias, o, cout, n0, D, H, W); break;
+        }
+    }
+    KV_CHECK_LAUNCH(ctx, "kv_conv3_bf16 (mma.sync)");
+    return KV_OK;
+}

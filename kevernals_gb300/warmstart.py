@@ -18,6 +18,7 @@ CLI (writes a checkpoint and a JSON report):
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import time
@@ -107,14 +108,31 @@ def shift_and_add_volume(plan, p):
     import torch
     c = getattr(plan, "_warm_cache", None)
     if c is not None:
-        a1, sens = c["a1"], c["sens"]
-        r = torch.where(a1 > 0, p / torch.where(a1 > 0, a1, torch.ones_like(a1)), torch.zeros_like(p))
-        b = plan.back(r.contiguous())
-        return torch.where(sens > 0, b.double() / torch.where(sens > 0, sens, torch.ones_like(sens)),
-                           torch.zeros_like(sens)).float()
+        return _saa_from_prepared(plan, c, p)[0]
     x = torch.zeros(plan.geometry.volume_shape, dtype=torch.float32, device=p.device)
     plan.sart(p, x, 1, 1.0)
     return x
+
+
+def _saa_from_prepared(plan, c, p):
+    """A^T(p / A1) / A^T 1 from the prepared A1 and A^T 1 with the engine's
+    kernels (ray ratio, backprojection, FP64 normalisation), and the uniform
+    start's data residual ||A1 - p|| / ||p||, which the ratio pass computes
+    on the way."""
+    import torch
+    from ._lib import lib
+    ctx = plan.ctx
+    p = p.contiguous()
+    r = torch.empty_like(p)
+    res = C.c_double()
+    ctx.use_torch_stream()
+    ctx.check(lib().kv_warm_ratio(ctx.handle, C.c_void_p(p.data_ptr()), C.c_void_p(c["a1"].data_ptr()),
+                                  C.c_void_p(r.data_ptr()), p.numel(), C.byref(res)))
+    b = plan.back(r)
+    out = torch.empty_like(b)
+    ctx.check(lib().kv_warm_normalize(ctx.handle, C.c_void_p(b.data_ptr()), C.c_void_p(c["sens"].data_ptr()),
+                                      C.c_void_p(out.data_ptr()), b.numel()))
+    return out, res.value
 
 
 def window_params(seed, offset_mm, n_ellipsoids=400):
@@ -184,7 +202,7 @@ def prepare(plan):
         sens = plan.sensitivity(device=True)
         pos = sens[sens > 0]
         seen = sens >= SEEN_FRACTION * float(pos.float().median()) if pos.numel() else sens > 0
-        c = {"a1": a1, "sens": sens, "seen": seen}
+        c = {"a1": a1, "sens": sens, "seen": seen, "seen_u8": seen.to(torch.uint8).contiguous()}
         plan._warm_cache = c
     return c
 
@@ -274,13 +292,16 @@ def iterations_to_residual(plan, p, x, target, max_iters, reject_above=None):
 def _start_estimate(plan, net, p):
     """The network's start (blind spots filled from the shift-and-add volume)
     and the uniform start's residual from the prepared A1."""
+    import torch
+    from ._lib import lib
     c = prepare(plan)
-    s = shift_and_add_volume(plan, p)
-    x0 = net.forward(s).clamp_(min=EPS)
-    unseen = ~c["seen"]
-    x0[unseen] = s[unseen].clamp(min=EPS)
-    pd = p.double()
-    r_u = float((c["a1"].double() - pd).norm() / pd.norm())
+    s, r_u = _saa_from_prepared(plan, c, p)
+    y = net.forward(s)
+    x0 = torch.empty_like(y)
+    ctx = plan.ctx
+    ctx.check(lib().kv_warm_fill(ctx.handle, C.c_void_p(y.data_ptr()), C.c_void_p(s.data_ptr()),
+                                 C.c_void_p(c["seen_u8"].data_ptr()), float(EPS), C.c_void_p(x0.data_ptr()),
+                                 x0.numel()))
     return x0, r_u
 
 

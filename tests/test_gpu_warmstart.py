@@ -65,3 +65,34 @@ def test_learned_warm_start_gains_over_plain_mlem():
         assert acc
         assert n_net < n_uniform
     assert sum(r[2] for r in results) <= sum(r[1] for r in results)
+
+
+def test_warm_start_elementwise_kernels_match_their_definitions():
+    """The warm start's ray ratio, FP64 normalisation and blind-spot fill
+    (kv_warm_ratio / kv_warm_normalize / kv_warm_fill) against the same
+    formulas in PyTorch, bit for bit; the uniform start's residual against
+    an FP64 norm."""
+    build.build()
+    ctx = engine.Context(0)
+    g = geom()
+    plan = engine.Plan(ctx, g, "exact")
+    params = ph.ellipsoid_params(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 10, ph.seed_for(5, 1))
+    truth = engine.phantom(ctx, g, params, device=True)
+    p = ws.noisy_data(ctx, plan, truth, 5e4, 3)
+    c = ws.prepare(plan)
+    s, r_u = ws._saa_from_prepared(plan, c, p)
+    a1, sens = c["a1"], c["sens"]
+    r = torch.where(a1 > 0, p / torch.where(a1 > 0, a1, torch.ones_like(a1)), torch.zeros_like(p))
+    b = plan.back(r.contiguous())
+    want = torch.where(sens > 0, b.double() / torch.where(sens > 0, sens, torch.ones_like(sens)),
+                       torch.zeros_like(sens)).float()
+    assert torch.equal(s, want)
+    pd = p.double()
+    assert r_u == pytest.approx(float((a1.double() - pd).norm() / pd.norm()), rel=1e-12)
+    net = engine.UNet(ctx, seed=0)
+    x0, r_u2 = ws._start_estimate(plan, net, p)
+    y = net.forward(s)
+    want0 = torch.where(c["seen"], y, s).clamp(min=ws.EPS)
+    assert torch.equal(x0, want0) and r_u2 == r_u
+    net.close()
+    plan.close()
