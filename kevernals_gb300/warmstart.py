@@ -481,12 +481,15 @@ def _cli():
                 g = config_chest() if (nx, ny, nz) == (1024, 1024, 128) else \
                     linear_sweep(nx, ny, nz, 0.4, 0.4, 2.5, 60, 2 * nx, 2 * ny, 0.2, 0.2, 17.5)
                 cases.append(evaluate_case(ctx, net, g, seed, max_iters=args.max_iters))
-        for c in cases:
-            log(json.dumps(c))
+            log(json.dumps(cases[-1]))
         sp = [c["speedup"] for c in cases if c["speedup"]]
-        report = {"cases": cases, "case_size": [nx, ny, nz],
+        report = {"cases": cases, "case_size": [nx, ny, nz], "checkpoint": args.ckpt,
                   "reached": sum(c["reached"] for c in cases), "accepted": sum(c["warm_accepted"] for c in cases),
-                  "median_speedup": float(np.median(sp)) if sp else None}
+                  "median_speedup": float(np.median(sp)) if sp else None,
+                  "min_speedup": float(np.min(sp)) if sp else None,
+                  "max_speedup": float(np.max(sp)) if sp else None,
+                  "at_least_3x": sum(1 for v in sp if v >= 3.0),
+                  "median_warm_iters": float(np.median([c["warm_iters"] for c in cases]))}
     with open(os.path.join(args.out, f"{args.cmd}_report.json"), "w") as f:
         json.dump(report, f, indent=1)
     log(json.dumps({k: v for k, v in report.items() if k != "cases"}))
