@@ -404,6 +404,67 @@ inline bool number(const Node *n, double &v) {
 
 }  // namespace kvxml
 
+class TomoGeometry;
+
+// Read-only views of a geometry's parts under the reference's class names,
+// as TomoGeometry::GetVolume / GetProjections / GetProjectionsRois /
+// GetTable return them (TomoGeometry.h:86-89): the value accessors of
+// TomoVolume (TomoVolume.h:49-64), TomoProjectionsSet
+// (TomoProjectionsSet.h:32-41) and TomoTable (TomoTable.h:16-23), read from
+// the owning TomoGeometry when called (so they follow its changes).  The
+// reference's setters, point-location helpers and RemoveProjection /
+// RemoveSource are not provided: the geometry changes through TomoGeometry.
+class TomoVolume {
+public:
+    explicit TomoVolume(const TomoGeometry *g = nullptr) : m_g(g) {}
+    int GetVoxelsNumber() const;
+    float GetSize() const;
+    Size3D GetSize3D() const;
+    WSize3D GetWSize3D() const;
+    Position3D GetBottomLeftFront() const;
+    Position3D GetTopRightBack() const;
+    VoxelSpacing GetVoxelSpacing() const;
+    std::vector<float> GetXPositions() const;
+    std::vector<float> GetYPositions() const;
+    std::vector<float> GetZPositions() const;
+    std::vector<Position3D> GetGridPositions() const;
+    std::vector<int> GetVoxelsIndices() const;
+
+private:
+    const TomoGeometry *m_g;
+};
+
+class TomoProjectionsSet {
+public:
+    explicit TomoProjectionsSet(const TomoGeometry *g = nullptr, bool rois = false) : m_g(g), m_rois(rois) {}
+    std::vector<Position2D> GetBottomLeftPositions() const;
+    Size2D GetSize() const;
+    WSize2D GetWSize() const;
+    PixelSpacing GetPixelSpacing() const;
+    std::vector<std::vector<float>> GetXPositions() const;
+    std::vector<std::vector<float>> GetYPositions() const;
+    std::vector<Position2D> GetProjectionPositions() const;
+    std::vector<int> GetProjectionPixelsIndices() const;
+    int GetNProjections() const;
+
+private:
+    const TomoGeometry *m_g;
+    bool m_rois;
+};
+
+class TomoTable {
+public:
+    explicit TomoTable(const TomoGeometry *g = nullptr) : m_g(g) {}
+    int GetSourcesNumber() const;
+    std::vector<float> GetSourcesYPositions() const;
+    float GetSourcesXCommonPosition() const;
+    float GetSourcesZCommonPosition() const;
+    float GetDetectorsZCommonPosition() const;
+
+private:
+    const TomoGeometry *m_g;
+};
+
 class TomoGeometry {
 public:
     // Reads a geometry file of the reference's format (TomoGeometry.cpp:13-434):
@@ -704,6 +765,25 @@ public:
     // the geometry file read ("" when built from values)
     std::string filePath() const { return m_filePath; }
 
+    // The parts (TomoGeometry.h:86-89), as read-only views owned by this
+    // geometry: valid while it lives, and they read its current values.
+    TomoVolume *GetVolume() const {
+        m_volumeView = TomoVolume(this);
+        return &m_volumeView;
+    }
+    TomoProjectionsSet *GetProjections() const {
+        m_projectionsView = TomoProjectionsSet(this, false);
+        return &m_projectionsView;
+    }
+    TomoProjectionsSet *GetProjectionsRois() const {
+        m_roisView = TomoProjectionsSet(this, true);
+        return &m_roisView;
+    }
+    TomoTable *GetTable() const {
+        m_tableView = TomoTable(this);
+        return &m_tableView;
+    }
+
     // Flattened description the kernels consume (Projector.cu:917-940):
     // sources (common x, y_i, common z), ROI origins (x_i, y_i, common z).
     struct Flat {
@@ -766,7 +846,60 @@ private:
     bool m_valid = false;
     std::string m_error;
     std::string m_filePath;
+    mutable TomoVolume m_volumeView;
+    mutable TomoProjectionsSet m_projectionsView, m_roisView;
+    mutable TomoTable m_tableView;
 };
+
+inline int TomoVolume::GetVoxelsNumber() const {
+    const Size3D n = m_g->volumeSize3D();
+    return n.x * n.y * n.z;
+}
+inline float TomoVolume::GetSize() const { return m_g->volumeSize(); }
+inline Size3D TomoVolume::GetSize3D() const { return m_g->volumeSize3D(); }
+inline WSize3D TomoVolume::GetWSize3D() const { return m_g->volumeWSize3D(); }
+inline Position3D TomoVolume::GetBottomLeftFront() const { return m_g->volumeBLF(); }
+inline Position3D TomoVolume::GetTopRightBack() const { return m_g->volumeTRB(); }
+inline VoxelSpacing TomoVolume::GetVoxelSpacing() const { return m_g->volumeVoxelSpacing(); }
+inline std::vector<float> TomoVolume::GetXPositions() const { return m_g->volumeXs(); }
+inline std::vector<float> TomoVolume::GetYPositions() const { return m_g->volumeYs(); }
+inline std::vector<float> TomoVolume::GetZPositions() const { return m_g->volumeZs(); }
+inline std::vector<Position3D> TomoVolume::GetGridPositions() const { return m_g->volumeGridPositions(); }
+inline std::vector<int> TomoVolume::GetVoxelsIndices() const { return m_g->volumeVoxelsIndices(); }
+
+inline std::vector<Position2D> TomoProjectionsSet::GetBottomLeftPositions() const {
+    return m_rois ? m_g->projectionsRoisBottomLeftPositions() : m_g->projectionsBottomLeftPositions();
+}
+inline Size2D TomoProjectionsSet::GetSize() const {
+    return m_rois ? m_g->projectionsRoisSize() : m_g->projectionsSize();
+}
+inline WSize2D TomoProjectionsSet::GetWSize() const {
+    return m_rois ? m_g->projectionsRoisWSize() : m_g->projectionsWSize();
+}
+inline PixelSpacing TomoProjectionsSet::GetPixelSpacing() const {
+    return m_rois ? m_g->projectionsRoisPixelSpacing() : m_g->projectionsPixelSpacing();
+}
+inline std::vector<std::vector<float>> TomoProjectionsSet::GetXPositions() const {
+    return m_rois ? m_g->projectionsRoisXPositions() : m_g->projectionsXPositions();
+}
+inline std::vector<std::vector<float>> TomoProjectionsSet::GetYPositions() const {
+    return m_rois ? m_g->projectionsRoisYPositions() : m_g->projectionsYPositions();
+}
+inline std::vector<Position2D> TomoProjectionsSet::GetProjectionPositions() const {
+    return m_rois ? m_g->projectionsRoisPositions() : m_g->projectionsPositions();
+}
+inline std::vector<int> TomoProjectionsSet::GetProjectionPixelsIndices() const {
+    return m_rois ? m_g->projectionsRoisPositionsIndices() : m_g->projectionsPositionsIndices();
+}
+inline int TomoProjectionsSet::GetNProjections() const {
+    return static_cast<int>(GetBottomLeftPositions().size());
+}
+
+inline int TomoTable::GetSourcesNumber() const { return m_g->nbProjections(); }
+inline std::vector<float> TomoTable::GetSourcesYPositions() const { return m_g->sourcesYPositions(); }
+inline float TomoTable::GetSourcesXCommonPosition() const { return m_g->sourcesXCommonPosition(); }
+inline float TomoTable::GetSourcesZCommonPosition() const { return m_g->sourcesZCommonPosition(); }
+inline float TomoTable::GetDetectorsZCommonPosition() const { return m_g->detectorsZCommonPosition(); }
 
 // A readable summary under the reference printer's headings
 // (TomoGeometry.h:119-125): volume, projections, projections Rois, table.

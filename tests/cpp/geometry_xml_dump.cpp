@@ -2,7 +2,8 @@
 // prints the flattened description the kernels receive, as JSON.  With
 // "adapt i j ..." after the path it first applies
 // PerformCheatingAdaptationsForDemonstration({i, j, ...}); with "accessors"
-// as the last argument it prints the geometry accessors instead.
+// as the last argument it prints the geometry accessors instead, with
+// "views" whether the part views (GetVolume, ...) agree with them.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -69,6 +70,60 @@ static int accessors(const TomoGeometry &g) {
     return 0;
 }
 
+template <typename A, typename B> static bool same(const A &a, const B &b) { return a == b; }
+static bool same(const Position2D &a, const Position2D &b) { return a.x == b.x && a.y == b.y; }
+static bool same(const Position3D &a, const Position3D &b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+static bool same(const Size2D &a, const Size2D &b) { return a.x == b.x && a.y == b.y; }
+static bool same(const Size3D &a, const Size3D &b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+static bool same(const PixelSpacing &a, const PixelSpacing &b) { return a.x == b.x && a.y == b.y; }
+static bool same(const VoxelSpacing &a, const VoxelSpacing &b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+template <typename T> static bool same(const std::vector<T> &a, const std::vector<T> &b) {
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+        if (!same(a[i], b[i])) return false;
+    return true;
+}
+
+// The part views (GetVolume / GetProjections / GetProjectionsRois /
+// GetTable) against the geometry's own accessors, printed as JSON booleans.
+static int views(const TomoGeometry &g) {
+    const TomoVolume *v = g.GetVolume();
+    const TomoProjectionsSet *d = g.GetProjections(), *r = g.GetProjectionsRois();
+    const TomoTable *t = g.GetTable();
+    const Size3D n = g.volumeSize3D();
+    const bool vol = v->GetVoxelsNumber() == n.x * n.y * n.z && v->GetSize() == g.volumeSize() &&
+                     same(v->GetSize3D(), n) && same(v->GetWSize3D(), g.volumeWSize3D()) &&
+                     same(v->GetBottomLeftFront(), g.volumeBLF()) && same(v->GetTopRightBack(), g.volumeTRB()) &&
+                     same(v->GetVoxelSpacing(), g.volumeVoxelSpacing()) && same(v->GetXPositions(), g.volumeXs()) &&
+                     same(v->GetYPositions(), g.volumeYs()) && same(v->GetZPositions(), g.volumeZs()) &&
+                     same(v->GetGridPositions(), g.volumeGridPositions()) &&
+                     same(v->GetVoxelsIndices(), g.volumeVoxelsIndices());
+    const bool det = same(d->GetBottomLeftPositions(), g.projectionsBottomLeftPositions()) &&
+                     same(d->GetSize(), g.projectionsSize()) && same(d->GetWSize(), g.projectionsWSize()) &&
+                     same(d->GetPixelSpacing(), g.projectionsPixelSpacing()) &&
+                     same(d->GetXPositions(), g.projectionsXPositions()) &&
+                     same(d->GetYPositions(), g.projectionsYPositions()) &&
+                     d->GetNProjections() == g.nbProjections();
+    const bool roi = same(r->GetBottomLeftPositions(), g.projectionsRoisBottomLeftPositions()) &&
+                     same(r->GetSize(), g.projectionsRoisSize()) && same(r->GetWSize(), g.projectionsRoisWSize()) &&
+                     same(r->GetPixelSpacing(), g.projectionsRoisPixelSpacing()) &&
+                     same(r->GetXPositions(), g.projectionsRoisXPositions()) &&
+                     same(r->GetYPositions(), g.projectionsRoisYPositions()) &&
+                     same(r->GetProjectionPositions(), g.projectionsRoisPositions()) &&
+                     same(r->GetProjectionPixelsIndices(), g.projectionsRoisPositionsIndices()) &&
+                     r->GetNProjections() == g.nbProjectionsRois();
+    const bool tab = t->GetSourcesNumber() == g.nbProjections() &&
+                     same(t->GetSourcesYPositions(), g.sourcesYPositions()) &&
+                     t->GetSourcesXCommonPosition() == g.sourcesXCommonPosition() &&
+                     t->GetSourcesZCommonPosition() == g.sourcesZCommonPosition() &&
+                     t->GetDetectorsZCommonPosition() == g.detectorsZCommonPosition();
+    std::printf("{\"volume\": %s, \"projections\": %s, \"rois\": %s, \"table\": %s, \"voxels\": %d, "
+                "\"views\": %d}\n",
+                vol ? "true" : "false", det ? "true" : "false", roi ? "true" : "false", tab ? "true" : "false",
+                v->GetVoxelsNumber(), d->GetNProjections());
+    return 0;
+}
+
 int main(int argc, char **argv) {
     if (argc < 2) return 2;
     TomoGeometry geo{std::string(argv[1])};
@@ -77,12 +132,14 @@ int main(int argc, char **argv) {
         return 0;
     }
     const bool show_accessors = std::string(argv[argc - 1]) == "accessors";
+    const bool show_views = std::string(argv[argc - 1]) == "views";
     if (argc > 2 && std::string(argv[2]) == "adapt") {
         std::vector<int> remove;
-        for (int i = 3; i < argc - (show_accessors ? 1 : 0); ++i) remove.push_back(std::atoi(argv[i]));
+        for (int i = 3; i < argc - (show_accessors || show_views ? 1 : 0); ++i) remove.push_back(std::atoi(argv[i]));
         geo.PerformCheatingAdaptationsForDemonstration(remove);
     }
     if (show_accessors) return accessors(geo);
+    if (show_views) return views(geo);
     const auto f = geo.flatten();
     const kv_geometry &g = f->g;
     std::printf("{\"valid\": true, \"n\": [%d, %d, %d], \"d\": [%.9g, %.9g, %.9g], \"views\": %d, "

@@ -349,3 +349,17 @@ def test_xml_invalid_files_match_reference_reader(dumper, ref_reader, tmp_path):
                {"rois": ["10 20 0 0 89 79"] * 2 + ["11 20 0 0 89 79"] + ["10 20 0 0 89 79"] * 2}):
         write_xml(path, **kw)
         assert not read(dumper, path)["valid"] and not json.loads(G.last_json([ref_reader, path]))["valid"], kw
+
+
+def test_geometry_part_views(dumper, tmp_path):
+    """GetVolume / GetProjections / GetProjectionsRois / GetTable
+    (TomoGeometry.h:86-89): read-only views whose accessors (the reference's
+    TomoVolume, TomoProjectionsSet and TomoTable getters) return exactly the
+    geometry's own values, before and after the demonstration adaptation."""
+    path = str(tmp_path / "geo.xml")
+    write_xml(path, res=(3, 4, 5), roi="1 2 0 0 6 5")
+    for extra in ([], ["adapt", "1"]):
+        got = json.loads(subprocess.run([dumper, path, *extra, "views"], check=True, capture_output=True,
+                                        text=True).stdout)
+        assert got["volume"] and got["projections"] and got["rois"] and got["table"], got
+    assert got["voxels"] == 5 * 4 * 100 and got["views"] == 4
