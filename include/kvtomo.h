@@ -239,9 +239,10 @@ kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int slices, int s
  * Projector.cu:376-785, on the EXACT path): voxel rows per thread share each
  * thread's candidate-column intervals, and consecutive slices per thread
  * are summed view by view so that they reuse each view's detector patch
- * from cache.  Shapes (rows, slices): (1, 1), (2, 1), (2, 2); rows 0 selects
+ * from cache.  Shapes (rows, slices): (1, 1), (2, 1), (2, 2), (4, 1),
+ * (4, 2), (8, 1); all give bit-identical volumes.  Rows 0 selects
  * one voxel per thread in blocks of 32 x back_rows of kv_plan_set_tuning.
- * Default (2, 2). */
+ * Default (8, 1). */
 kv_status kv_plan_get_back_shape(const kv_plan *plan, int *rows_per_thread, int *slices_per_thread);
 kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_per_thread);
 

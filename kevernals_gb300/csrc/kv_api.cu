@@ -1047,10 +1047,12 @@ extern "C" kv_status kv_plan_get_back_shape(const kv_plan *plan, int *rows_per_t
 extern "C" kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_per_thread) {
     if (plan == nullptr) return KV_ERR_INVALID_ARG;
     const bool ok = rows_per_thread == 0 || (rows_per_thread == 1 && slices_per_thread == 1) ||
-                    (rows_per_thread == 2 && (slices_per_thread == 1 || slices_per_thread == 2));
+                    ((rows_per_thread == 2 || rows_per_thread == 4) &&
+                     (slices_per_thread == 1 || slices_per_thread == 2)) ||
+                    (rows_per_thread == 8 && slices_per_thread == 1);
     if (!ok)
         return kv_fail(plan->ctx, KV_ERR_INVALID_ARG,
-                       "gather backprojector shape must be rows 0, (1, 1), (2, 1) or (2, 2)");
+                       "gather backprojector shape must be rows 0, (1, 1), (2, 1), (2, 2), (4, 1), (4, 2) or (8, 1)");
     if (rows_per_thread == 0) slices_per_thread = 1;
     plan->back_rows = rows_per_thread;
     plan->back_slices = slices_per_thread;

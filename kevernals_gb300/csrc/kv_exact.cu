@@ -443,8 +443,11 @@ __global__ void __launch_bounds__(256) exact_back_kernel(ExGeom G, ExactTables T
 // L1.  For each (view, slice) a lane computes the x-intervals of its voxel
 // column's candidate detector columns once -- only as many slots as the
 // warp's widest voxel needs -- and uses them for its R voxel rows; the
-// candidate detector rows of each voxel row go to shared memory as
-// t-intervals, one lane per candidate; the R voxel rows then run through
+// candidate detector rows of the R voxel rows go to shared memory as
+// t-intervals, computed side by side (lane group q of 32/R lanes evaluates
+// row q's range and intervals, one lane per candidate, so a warp fills all R
+// rows in one pass when each has at most 32/R candidates); the pairs are
+// visited in the same order for every R.  The R voxel rows then run through
 // their candidate rows in lockstep (independent accumulators, so their loads
 // and sums overlap).  Weights are the same float expressions as back_tile's,
 // bit for bit.
@@ -466,7 +469,9 @@ __device__ __forceinline__ void back_chunk_r(const ExGeom &G, const ExactTables 
             const float4 X = T.xt[(size_t)p * G.nu + u];
             const int ib = T.xi[(size_t)p * G.nu + u];
             const float ftx = __fmaf_rn(X.y, htop, X.x);
-            const float ta = cross_t(i - ib, ftx, X.z), tb = cross_t(i + 1 - ib, ftx, X.z);
+            // the two bounding planes as exact float integers (one conversion)
+            const float fi = (float)(i - ib);
+            const float ta = cross_tf(fi, ftx, X.z), tb = cross_tf(__fadd_rn(fi, 1.f), ftx, X.z);
             lox[s] = fmaxf(0.f, fminf(ta, tb));
             hix[s] = fminf(1.f, fmaxf(ta, tb));
         }
@@ -485,12 +490,15 @@ __device__ __forceinline__ void back_chunk_r(const ExGeom &G, const ExactTables 
     }
 }
 
-template <typename VolT, typename ProjT, int ACC, int MODE, int R, int S>
+template <typename VolT, typename ProjT, int ACC, int R, int S>
 __device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &T, const BackArgs &a,
-                                            double *sens_out, int bx, int by, int k0, int kend) {
+                                            double *sens_out, int bx, int by, int k0, int kend, int mode) {
+    constexpr int CW = 32 / R;                 // candidates of one voxel row filled per pass
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int i = bx * 32 + lane;
     const int jw = by * 8 * R + warp;          // voxel row of q = 0; rows jw + 8q
+    const int qf = lane / CW, cf = lane % CW;  // this lane fills candidate cf (+ CW f) of row qf
+    const int jf = jw + 8 * qf;
     __shared__ float2 ysh[8][R][32];
     const bool live_i = i < G.nx;
     const ProjT *yp = static_cast<const ProjT *>(a.yp);
@@ -514,41 +522,40 @@ __device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &
             int u1 = min(G.nu - 1, (int)floorf(fmaxf(ulo, uhi) + 0.01f));
             if (!live_i) u1 = u0 - 1;
             const int n_u_warp = __reduce_max_sync(0xffffffffu, u1 >= u0 ? u1 - u0 + 1 : 0);
-            // candidate detector rows of each voxel row (warp-uniform)
-            int v0[R], nvr[R], nvmax = 0;
-#pragma unroll
-            for (int q = 0; q < R; ++q) {
-                const int j = jw + 8 * q;
-                nvr[q] = 0;
-                v0[q] = 0;
-                if (j < G.ny) {
-                    const float vlo = fminf(((float)j - r0.z) * r0.w, ((float)j - r1.z) * r1.w);
-                    const float vhi = fmaxf(((float)(j + 1) - r0.z) * r0.w, ((float)(j + 1) - r1.z) * r1.w);
-                    v0[q] = max(0, (int)ceilf(fminf(vlo, vhi) - 0.01f));
-                    const int v1 = min(G.nv - 1, (int)floorf(fmaxf(vlo, vhi) + 0.01f));
-                    nvr[q] = max(0, v1 - v0[q] + 1);
-                }
-                nvmax = max(nvmax, nvr[q]);
+            // candidate detector rows of the lane's fill row: the R rows are
+            // evaluated side by side in lane groups of CW, and each row's first
+            // candidate is broadcast from the first lane of its group
+            int v0f = 0, nvf = 0;
+            if (jf < G.ny) {
+                const float vlo = fminf(((float)jf - r0.z) * r0.w, ((float)jf - r1.z) * r1.w);
+                const float vhi = fmaxf(((float)(jf + 1) - r0.z) * r0.w, ((float)(jf + 1) - r1.z) * r1.w);
+                v0f = max(0, (int)ceilf(fminf(vlo, vhi) - 0.01f));
+                const int v1 = min(G.nv - 1, (int)floorf(fmaxf(vlo, vhi) + 0.01f));
+                nvf = max(0, v1 - v0f + 1);
             }
-            for (int vb = 0; vb < nvmax; vb += 32) {
-                // the rows' candidate intervals, one lane per candidate; entries past
-                // a row's candidates are empty (lo > hi) and weigh nothing
+            const int nvmax = __reduce_max_sync(0xffffffffu, nvf);
+            int v0[R];
 #pragma unroll
-                for (int q = 0; q < R; ++q) {
+            for (int q = 0; q < R; ++q) v0[q] = __shfl_sync(0xffffffffu, v0f, q * CW);
+            for (int vb = 0; vb < nvmax; vb += 32) {
+                const int nvc = min(32, nvmax - vb);
+                // the rows' candidate intervals, CW candidates of each row per pass;
+                // entries past a row's candidates are empty (lo > hi) and weigh nothing
+                for (int f = 0; f * CW < nvc; ++f) {
                     float2 iv = make_float2(1.f, 0.f);
-                    const int c = vb + lane;
-                    if (c < nvr[q]) {
-                        const int vv = v0[q] + c, j = jw + 8 * q;
+                    const int c = vb + f * CW + cf;
+                    if (c < nvf) {
+                        const int vv = v0f + c;
                         const float4 Y = T.yt[(size_t)p * G.nv + vv];
                         const int jb = T.yi[(size_t)p * G.nv + vv];
                         const float fty = __fmaf_rn(Y.y, htop, Y.x);
-                        const float ta = cross_t(j - jb, fty, Y.z), tb = cross_t(j + 1 - jb, fty, Y.z);
+                        const float fj = (float)(jf - jb);
+                        const float ta = cross_tf(fj, fty, Y.z), tb = cross_tf(__fadd_rn(fj, 1.f), fty, Y.z);
                         iv = make_float2(fmaxf(0.f, fminf(ta, tb)), fminf(1.f, fmaxf(ta, tb)));
                     }
-                    ysh[warp][q][lane] = iv;
+                    ysh[warp][qf][f * CW + cf] = iv;
                 }
                 __syncwarp();
-                const int nvc = min(32, nvmax - vb);
                 for (int cb = 0; cb * BACK_SLOTS < n_u_warp; ++cb) {
                     const int ub = u0 + cb * BACK_SLOTS;
                     const int nslot = min(BACK_SLOTS, n_u_warp - cb * BACK_SLOTS);
@@ -588,13 +595,13 @@ __device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &
             }
             VolT *vol = static_cast<VolT *>(a.vol);
             const float b = (float)acc[kk][q];
-            if (MODE == BACK_PLAIN) {
+            if (mode == BACK_PLAIN) {
                 Store<VolT>::st(vol + idx, b);
-            } else if (MODE == BACK_MLEM) {
+            } else if (mode == BACK_MLEM) {
                 const double sv = a.sens[idx];
                 if (sv > 0.0)
                     Store<VolT>::st(vol + idx, (float)((double)Store<VolT>::ld_rw(vol + idx) * (double)b / sv));
-            } else if (MODE == BACK_SART) {
+            } else if (mode == BACK_SART) {
                 const double sv = a.sens[idx];
                 if (sv > 0.0)
                     Store<VolT>::st(vol + idx, Store<VolT>::ld_rw(vol + idx) + (float)((double)(a.relax * b) / sv));
@@ -608,11 +615,13 @@ __device__ __forceinline__ void back_tile_r(const ExGeom &G, const ExactTables &
 // in flight cover a strip of voxel columns at every height, whose detector
 // footprint over all views stays in L2 while the strip's rows are swept
 // (slice groups slowest re-read every projection image once per group).
-template <typename VolT, typename ProjT, int ACC, int MODE, int R, int S>
+// The pass (plain, MLEM update, SART update) only changes the epilogue: a
+// kernel argument, not a template parameter.
+template <typename VolT, typename ProjT, int ACC, int R, int S>
 __global__ void __launch_bounds__(256) exact_back_r_kernel(ExGeom G, ExactTables T, BackArgs a,
-                                                           double *sens_out, int z0, int nzs) {
-    back_tile_r<VolT, ProjT, ACC, MODE, R, S>(G, T, a, sens_out, blockIdx.z, blockIdx.y, z0 + S * (int)blockIdx.x,
-                                              z0 + nzs);
+                                                           double *sens_out, int z0, int nzs, int mode) {
+    back_tile_r<VolT, ProjT, ACC, R, S>(G, T, a, sens_out, blockIdx.z, blockIdx.y, z0 + S * (int)blockIdx.x,
+                                        z0 + nzs, mode);
 }
 
 ExGeom exgeom(const kv_plan *plan, int n_views) {
@@ -741,20 +750,19 @@ template <typename VolT, typename ProjT, int ACC, int R, int S>
 void back_r_launch(const ExGeom &G, const ExactTables &t, BackMode mode, const BackArgs &a, double *sens_out,
                    int z0, int nzs, cudaStream_t st) {
     dim3 block(32, 8), grid((nzs + S - 1) / S, (G.ny + 8 * R - 1) / (8 * R), (G.nx + 31) / 32);
-    switch (mode) {
-    case BACK_PLAIN: exact_back_r_kernel<VolT, ProjT, ACC, BACK_PLAIN, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
-    case BACK_MLEM: exact_back_r_kernel<VolT, ProjT, ACC, BACK_MLEM, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
-    case BACK_SART: exact_back_r_kernel<VolT, ProjT, ACC, BACK_SART, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs); break;
-    }
+    exact_back_r_kernel<VolT, ProjT, ACC, R, S><<<grid, block, 0, st>>>(G, t, a, sens_out, z0, nzs, (int)mode);
 }
 
-// (rows per thread, slices per thread): (1, 1), (2, 1) or (2, 2)
+// (rows per thread, slices per thread): (1, 1), (2, 1), (2, 2), (4, 1), (4, 2) or (8, 1)
 template <typename VolT, typename ProjT, int ACC>
 void back_r_dispatch(int R, int S, const ExGeom &G, const ExactTables &t, BackMode mode, const BackArgs &a,
                      double *sens_out, int z0, int nzs, cudaStream_t st) {
     if (R == 1) back_r_launch<VolT, ProjT, ACC, 1, 1>(G, t, mode, a, sens_out, z0, nzs, st);
-    else if (S == 1) back_r_launch<VolT, ProjT, ACC, 2, 1>(G, t, mode, a, sens_out, z0, nzs, st);
-    else back_r_launch<VolT, ProjT, ACC, 2, 2>(G, t, mode, a, sens_out, z0, nzs, st);
+    else if (R == 2 && S == 1) back_r_launch<VolT, ProjT, ACC, 2, 1>(G, t, mode, a, sens_out, z0, nzs, st);
+    else if (R == 2) back_r_launch<VolT, ProjT, ACC, 2, 2>(G, t, mode, a, sens_out, z0, nzs, st);
+    else if (R == 4 && S == 1) back_r_launch<VolT, ProjT, ACC, 4, 1>(G, t, mode, a, sens_out, z0, nzs, st);
+    else if (R == 4) back_r_launch<VolT, ProjT, ACC, 4, 2>(G, t, mode, a, sens_out, z0, nzs, st);
+    else back_r_launch<VolT, ProjT, ACC, 8, 1>(G, t, mode, a, sens_out, z0, nzs, st);
 }
 
 template <typename VolT, typename ProjT>
@@ -1241,7 +1249,7 @@ kv_status tune_shapes(kv_plan *plan, int P, TuneResult &best) {
     // gather backprojector: (rows, slices) per thread, or one voxel per thread
     const ExGeom G = exgeom(plan, P);
     const BackArgs ba{plan->d_ratio, plan->d_vol, nullptr, 1.f};
-    static const int bshapes[][2] = {{2, 2}, {2, 1}, {1, 1}};
+    static const int bshapes[][2] = {{8, 1}, {4, 1}, {4, 2}, {2, 1}, {2, 2}, {1, 1}};
     bt = 1e30f;
     for (const auto &sh : bshapes) {
         const float ms = median3(ctx, e0, e1, [&] {

@@ -58,7 +58,7 @@ struct SlabArgs {
     int S, BX, BY, stages, nslab, group, n_ut, n_vt, align;
     uint32_t stage_elems;            // elements between stages (BX * BY * S rounded up to 128 bytes)
     uint32_t stage_bytes;            // bytes one box load delivers: BX * BY * S * element size
-    uint32_t desc_off, hr_off, yt_off, yi_off;   // byte offsets in dynamic shared memory
+    uint32_t desc_off, hr_off, yt_off, yi_off, org_off;   // byte offsets in dynamic shared memory
     int *status;                     // error bits (0: fine)
 };
 
@@ -182,7 +182,6 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
     constexpr bool SART = MODE == FWD_SART;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t full[kMaxStages];
-    __shared__ int2 origin[kMaxStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     // ---- tile: detector columns u0 .. u0+31, rows v0 .. v0+TV-1 of view p
@@ -206,6 +205,7 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
     float *s_hr = reinterpret_cast<float *>(base + A.hr_off);         // [nz + 1]
     float4 *s_yt = reinterpret_cast<float4 *>(base + A.yt_off);       // [TV]
     int *s_yi = reinterpret_cast<int *>(base + A.yi_off);             // [TV]
+    int2 *org = reinterpret_cast<int2 *>(base + A.org_off);           // [nslab]: box origin of each slab
 
     for (int i = threadIdx.x; i <= G.nz; i += kThreads) s_hr[i] = T.hr[(size_t)p * (G.nz + 1) + i];
     if (threadIdx.x < TV) {
@@ -219,20 +219,29 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
     }
     __syncthreads();
 
-    const int ua = u0, ub = min(u0 + 31, G.nu - 1);
-    const int vb_local = min(TV - 1, G.nv - 1 - v0);
-    // thread 0: place and load the box of slab s into stage st
+    // the box of every slab, placed once before any load or row descriptor
+    // needs it (a box origin written while the pipeline runs would be read by
+    // the next slab's descriptors with no barrier in between at two stages)
+    {
+        const int ua = u0, ub = min(u0 + 31, G.nu - 1);
+        const int vb_local = min(TV - 1, G.nv - 1 - v0);
+        for (int s = threadIdx.x; s < A.nslab; s += kThreads) {
+            const int ks = s * A.S, ke = min(ks + A.S, G.nz);
+            const float4 Xa = T.xt[(size_t)p * G.nu + ua], Xb = T.xt[(size_t)p * G.nu + ub];
+            const int ia = T.xi[(size_t)p * G.nu + ua], ibb = T.xi[(size_t)p * G.nu + ub];
+            int x0, y0, nxn, nyn;
+            box_origin(Xa, ia, Xb, ibb, s_yt[0], s_yi[0], s_yt[vb_local], s_yi[vb_local], s_hr[ks], s_hr[ke],
+                       A.align, x0, y0, nxn, nyn);
+            org[s] = make_int2(x0, y0);
+        }
+    }
+    __syncthreads();
+    // thread 0: load the box of slab s into stage st
     auto issue = [&](int s, int st) {
-        const int ks = s * A.S, ke = min(ks + A.S, G.nz);
-        const float4 Xa = T.xt[(size_t)p * G.nu + ua], Xb = T.xt[(size_t)p * G.nu + ub];
-        const int ia = T.xi[(size_t)p * G.nu + ua], ibb = T.xi[(size_t)p * G.nu + ub];
-        int x0, y0, nxn, nyn;
-        box_origin(Xa, ia, Xb, ibb, s_yt[0], s_yi[0], s_yt[vb_local], s_yi[vb_local], s_hr[ks], s_hr[ke], A.align,
-                   x0, y0, nxn, nyn);
-        origin[st] = make_int2(x0, y0);
         kvtma::fence_proxy_async_smem();
         kvtma::mbar_arrive_expect_tx(&full[st], A.stage_bytes);
-        kvtma::tma_load_3d(kvtma::smem_u32(boxes + (size_t)st * A.stage_elems), &vmap, &full[st], x0, y0, ks);
+        kvtma::tma_load_3d(kvtma::smem_u32(boxes + (size_t)st * A.stage_elems), &vmap, &full[st], org[s].x, org[s].y,
+                           s * A.S);
     };
     // threads < S*TV: the row descriptors of slab s into buffer buf
     auto make_desc = [&](int s, int buf) -> int {
@@ -258,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
             const float y3 = cross_tf(p3, fty, Y.z), y4 = cross_tf(p4, fty, Y.z);
             const int nr = 1 + (y1 < 1.f) + (y2 < 1.f) + (y3 < 1.f) + (y4 < 1.f);
             const int j0 = s_yi[vl] + (int)fj;
-            const int js = j0 - origin[s % A.stages].y;
+            const int js = j0 - org[s].y;
             const int je = js + (negy ? 1 - nr : nr - 1);
             if (min(js, je) < 0 || max(js, je) >= A.BY) {
                 bad = 4;
@@ -308,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
         if (err == 0) {
             const unsigned char *box = reinterpret_cast<const unsigned char *>(boxes + (size_t)st * A.stage_elems);
             const YDesc *dsc = desc + (s & 1) * A.S * TV;
-            const int xoff = ib - origin[st].x;
+            const int xoff = ib - org[s].x;
             const int kend = min(A.S, G.nz - s * A.S);
             for (int kk = 0; kk < kend; ++kk) {
                 const float ftx = __fmaf_rn(X.y, s_hr[s * A.S + kk + 1], X.x);
@@ -415,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, R >= 8 ? 2 : 3) fwd_slab_kernel(cons
 // Dynamic shared memory layout of one CTA (byte offsets from the first
 // 128-byte aligned address of the region).
 struct SmemLayout {
-    uint32_t stage_stride, desc_off, hr_off, yt_off, yi_off;
+    uint32_t stage_stride, desc_off, hr_off, yt_off, yi_off, org_off;
     size_t total;
 };
 
@@ -432,7 +441,9 @@ SmemLayout smem_layout(int R, int S, int stages, int BX, int BY, int nz, int es)
     L.yt_off = (uint32_t)off;
     off += (size_t)TV * sizeof(float4);
     L.yi_off = (uint32_t)off;
-    off += (size_t)TV * sizeof(int);
+    off = up(off + (size_t)TV * sizeof(int), 8);
+    L.org_off = (uint32_t)off;
+    off += (size_t)((nz + S - 1) / S) * sizeof(int2);
     L.total = up(off, 128) + 128;   // + slack for aligning the region's start
     return L;
 }
@@ -574,6 +585,7 @@ kv_status fwd_slab_launch(kv_plan *plan, const ExactTables &t, int P, FwdMode mo
     A.hr_off = L.hr_off;
     A.yt_off = L.yt_off;
     A.yi_off = L.yi_off;
+    A.org_off = L.org_off;
     A.status = plan->ctx->d_status;
     const ExGeom G{g.nx, g.ny, g.nz, g.nu, g.nv, P};
     const unsigned grid = (unsigned)((size_t)A.n_ut * A.n_vt * P);

@@ -122,8 +122,8 @@ struct kv_plan {
     // launch tuning (set by kv_plan_autotune or defaults)
     int fwd_by = 4;                  // forward block = 32 x fwd_by rays
     int back_by = 8;                 // backprojector block = 32 x back_by voxels (one voxel per thread)
-    int back_rows = 2;               // voxel rows per thread of the gather backprojector (0: one voxel per thread)
-    int back_slices = 2;             // slices per thread of the gather backprojector
+    int back_rows = 8;               // voxel rows per thread of the gather backprojector (0: one voxel per thread)
+    int back_slices = 1;             // slices per thread of the gather backprojector
 
     // captured iteration loop (kv_mlem / kv_sart without callback), reused
     // while the buffers and parameters are the same

@@ -1,8 +1,13 @@
 """Every convolution shape of the U-Net, one layer at a time, through the C ABI
 (kv_conv3_bf16): the tcgen05 / TMA implicit GEMM against the mma.sync kernel
 (the same products summed in the same K order: bit-identical) and against an
-FP64 conv3d of the same BF16 inputs and weights (the only difference is the
-final rounding of the FP32 sums to BF16 and their summation order)."""
+FP64 conv3d of the same BF16 inputs and weights.  Against FP64 the output
+differs by the final rounding to BF16 (half an ulp) plus the error of the
+FP32 accumulation on the tensor cores, which align the products of each MMA
+step to the largest and truncate: measured 1e-6 .. 6e-6 absolute on sums of
+5184 products whose magnitudes add to ~50, so the bound is
+2^-8 |ref| + 2^-20 sum|w x|, and at least 99 % of the outputs must equal
+the FP64 value rounded to nearest even."""
 import ctypes as C
 
 import numpy as np
@@ -79,11 +84,16 @@ def test_conv_layer_tcgen05_vs_mma_sync_and_fp64(ctx, shape):
     xt = torch.from_numpy(x.astype(np.float64)).permute(3, 0, 1, 2)[None]
     wt = torch.from_numpy(wf.astype(np.float64)).permute(0, 2, 1).reshape(cout, cin, 3, 3, 3)
     ref = F.conv3d(xt, wt, torch.from_numpy(bias.astype(np.float64)), padding=1)
+    mag = F.conv3d(xt.abs(), wt.abs(), torch.from_numpy(np.abs(bias).astype(np.float64)), padding=1)
     if relu:
         ref = F.relu(ref)
     ref = ref[0].permute(1, 2, 3, 0).numpy()
+    mag = mag[0].permute(1, 2, 3, 0).numpy()
     got = (tc.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
-    # BF16 output: half an ulp of 2^-8 relative, plus the FP32 summation
     err = np.abs(got - ref)
-    assert np.all(err <= 2 ** -8 * np.abs(ref) + 1e-6), err.max()
+    bound = 2 ** -8 * np.abs(ref) + 2 ** -20 * mag
+    worst = np.unravel_index(np.argmax(err - bound), err.shape)
+    assert np.all(err <= bound), (worst, got[worst], ref[worst], mag[worst])
+    _, rne = _bf16_bits(ref.astype(np.float32))
+    assert np.mean(got == rne) > 0.99
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 4e-3

@@ -423,14 +423,17 @@ def test_back_shapes_bit_identical(ctx):
     """The gather backprojector's work shapes (voxel rows and slices per
     thread, or one voxel per thread) evaluate the same weights in the same
     order per voxel: identical volumes, and the FP64 oracle within tolerance;
-    likewise the FP64 sensitivity image."""
-    for g in small_geoms():
+    likewise the FP64 sensitivity image.  The last geometry's detector rows
+    are 40 times finer than its voxel rows (40-odd candidate rows per voxel
+    row), so the candidate intervals take several fill passes and row chunks."""
+    fine_rows = linear_sweep(24, 12, 6, 1.0, 2.0, 1.0, 5, 96, 640, 0.3, 0.05, 15.0)
+    for g in small_geoms() + [fine_rows]:
         y = np.random.default_rng(3).random(g.proj_shape, dtype=np.float32)
         ref = O.exact_back(g, y.astype(np.float64))
         plan = engine.Plan(ctx, g, "exact")
-        assert plan.back_shape == (2, 2)
+        assert plan.back_shape == (8, 1)
         outs, sens = [], []
-        for shape in [(0, 1), (1, 1), (2, 1), (2, 2)]:
+        for shape in [(0, 1), (1, 1), (2, 1), (2, 2), (4, 1), (4, 2), (8, 1)]:
             plan.set_back_shape(*shape)
             outs.append(plan.back(y))
             plan2 = engine.Plan(ctx, g, "exact")
@@ -444,6 +447,8 @@ def test_back_shapes_bit_identical(ctx):
         assert rel_l2(outs[0], ref) < EXACT_BACK_REL_L2
         with pytest.raises(KvError):
             plan.set_back_shape(1, 2)
+        with pytest.raises(KvError):
+            plan.set_back_shape(3, 1)
         plan.close()
 
 
