@@ -182,8 +182,30 @@ kv_status saa_shifts(kv_ctx *ctx, const kv_geometry &g, kv_family family, int32_
 }
 
 // Host-buffer calls overlap their copies with the kernels on a second
-// (non-blocking) stream of the context, in kOverlapChunks pieces.
+// (non-blocking) stream of the context, in at most kOverlapChunks pieces.
 constexpr int kOverlapChunks = 8;
+// A projector pass over one view or slice takes ~10-20x as long as copying
+// that view or slice at the host link's ~200 GB/s, so pieces may grow by
+// this factor and each copy still hides behind the previous piece's kernels.
+constexpr int kOverlapGrowth = 4;
+
+// Piece boundaries of [0, total): sizes 1, g, g^2, ... (the last piece takes
+// the rest), at most kOverlapChunks pieces.  Uploads use them in this order
+// (the first piece's copy is the only one that nothing hides); downloads
+// reversed (the last piece's copy is).  Few pieces keep the launches few.
+std::vector<int> overlap_bounds(int total, bool shrinking) {
+    std::vector<int> sizes;
+    int left = total;
+    for (long long sz = 1; left > 0; sz *= kOverlapGrowth) {
+        const int take = (int)sizes.size() == kOverlapChunks - 1 ? left : (int)std::min<long long>(sz, left);
+        sizes.push_back(take);
+        left -= take;
+    }
+    if (shrinking) std::reverse(sizes.begin(), sizes.end());
+    std::vector<int> b(1, 0);
+    for (int v : sizes) b.push_back(b.back() + v);
+    return b;
+}
 
 kv_status ensure_copy_stream(kv_ctx *ctx) {
     if (ctx->copy_stream == nullptr)
@@ -196,7 +218,7 @@ kv_status ensure_copy_stream(kv_ctx *ctx) {
     return KV_OK;
 }
 
-// Runs launch(i0, n) on the context stream for kOverlapChunks pieces of
+// Runs launch(i0, n) on the context stream for the (shrinking) pieces of
 // [0, total) and copies each piece's output (dev + i0 * stride, n * stride
 // floats) to the same place in host memory on the copy stream as soon as
 // that piece's kernels are done.  Events ev0 .. ev0 + kOverlapChunks - 1.
@@ -204,15 +226,16 @@ template <typename Launch>
 kv_status pieces_to_host_body(kv_ctx *ctx, int total, size_t stride, const float *dev, float *host, int ev0,
                               Launch &launch) {
     cudaEvent_t *ev = ctx->copy_events.data() + ev0;
-    const int pc = (total + kOverlapChunks - 1) / kOverlapChunks;
-    for (int c = 0, i0 = 0; i0 < total; i0 += pc, ++c) {
-        KV_TRY(launch(i0, std::min(pc, total - i0)));
+    const std::vector<int> b = overlap_bounds(total, true);
+    const int np = (int)b.size() - 1;
+    for (int c = 0; c < np; ++c) {
+        KV_TRY(launch(b[c], b[c + 1] - b[c]));
         KV_CHECK_CUDA(ctx, cudaEventRecord(ev[c], ctx->stream));
     }
-    for (int c = 0, i0 = 0; i0 < total; i0 += pc, ++c) {
-        const size_t n = (size_t)std::min(pc, total - i0) * stride;
+    for (int c = 0; c < np; ++c) {
+        const size_t n = (size_t)(b[c + 1] - b[c]) * stride;
         KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev[c], 0));
-        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(host + i0 * stride, dev + i0 * stride, n * sizeof(float),
+        KV_CHECK_CUDA(ctx, cudaMemcpyAsync(host + b[c] * stride, dev + b[c] * stride, n * sizeof(float),
                                            cudaMemcpyDeviceToHost, ctx->copy_stream));
     }
     return KV_OK;
@@ -816,11 +839,11 @@ kv_status iterate(kv_plan *plan, const void *p, void *x, int iters, float relax,
 }
 
 // Host-buffer MLEM / SART (both families, FP32 storage) without a callback.
-// The volume and then the projections, kOverlapChunks view chunks, go up on
-// the context's copy stream; the first forward projection runs chunk by
-// chunk, each chunk as soon as its projections have landed.  The last
-// backprojection runs in kOverlapChunks slabs of slices and each slab is
-// copied back while the next ones are computed.  Per ray and per voxel the
+// The volume and then the projections, in growing view chunks, go up on the
+// context's copy stream; the first forward projection runs chunk by chunk,
+// each chunk as soon as its projections have landed.  The last
+// backprojection runs in shrinking slabs of slices and each slab is copied
+// back while the next ones are computed.  Per ray and per voxel the
 // arithmetic is that of the whole-volume launches, so the result equals the
 // device-buffer call bit for bit.
 
@@ -854,9 +877,9 @@ kv_status overlapped_body(kv_plan *plan, const float *proj, float *volume, int i
     KV_CHECK_CUDA(ctx, cudaEventRecord(ev[0], st));
     KV_CHECK_CUDA(ctx, cudaStreamWaitEvent(cs, ev[0], 0));
     KV_CHECK_CUDA(ctx, cudaMemcpyAsync(xd, volume, plan->nvox * sizeof(float), cudaMemcpyHostToDevice, cs));
-    const int vc = (g.n_views + kOverlapChunks - 1) / kOverlapChunks;
-    for (int c = 0, v0 = 0; v0 < g.n_views; v0 += vc, ++c) {
-        const int n = std::min(vc, g.n_views - v0);
+    const std::vector<int> vb = overlap_bounds(g.n_views, false);
+    for (int c = 0; c + 1 < (int)vb.size(); ++c) {
+        const int v0 = vb[c], n = vb[c + 1] - vb[c];
         KV_CHECK_CUDA(ctx, cudaMemcpyAsync(pd + v0 * D, proj + v0 * D, n * D * sizeof(float),
                                            cudaMemcpyHostToDevice, cs));
         KV_CHECK_CUDA(ctx, cudaEventRecord(ev[1 + c], cs));

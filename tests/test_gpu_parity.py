@@ -275,9 +275,11 @@ def test_device_buffers_match_host(ctx):
 @pytest.mark.parametrize("gi", [0, 1, 2])
 def test_host_mlem_sart_overlapped_equal_device(ctx, gi, family):
     """Host-buffer MLEM / SART (FP32) overlap the copies with the first
-    forward projection (view chunks) and the last backprojection (slabs of
-    slices); the result equals the device-buffer call bit for bit for 1 to 4
-    iterations, with ragged chunks (5, 4 and 9 views; 12, 7 and 16 slices)."""
+    forward projection (view chunks growing 1, 4, 16, ...) and the last
+    backprojection (slabs of slices shrinking to 1); the result equals the
+    device-buffer call bit for bit for 1 to 4 iterations, with ragged pieces
+    (5 views: 1 + 4, 9 views: 1 + 4 + 4; 12 slices: 7 + 4 + 1, 16 slices:
+    11 + 4 + 1)."""
     torch = pytest.importorskip("torch")
     g = small_geoms()[gi]
     p = O.exact_forward(g, phantom_for(g).astype(np.float64)).astype(np.float32)
