@@ -246,6 +246,19 @@ kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int slices, int s
 kv_status kv_plan_get_back_shape(const kv_plan *plan, int *rows_per_thread, int *slices_per_thread);
 kv_status kv_plan_set_back_shape(kv_plan *plan, int rows_per_thread, int slices_per_thread);
 
+/* The EXACT backprojector with each view's detector patch staged in shared
+ * memory by TMA, one view ahead (no reference counterpart; it replaces the
+ * gather kernels of kv_plan_set_back_shape for FP32 storage when set): 4 or
+ * 8 voxel rows per thread, 2 or 3 stages; rows 0 turns it off.  Its volumes
+ * are bit-identical to the gather kernels'.  KV_ERR_UNSUPPORTED when the
+ * plan does not suit it (16-bit storage, detector rows that are not a whole
+ * number of 16 bytes, a voxel tile that sees more than 256 x 256 detector
+ * pixels, or patches beyond the shared-memory budget).  The getter also
+ * reports the patch size in detector columns and rows. */
+kv_status kv_plan_get_back_staging(const kv_plan *plan, int *rows_per_thread, int *stages, int *patch_cols,
+                                   int *patch_rows);
+kv_status kv_plan_set_back_staging(kv_plan *plan, int rows_per_thread, int stages);
+
 /* ---- learned warm start (no reference counterpart) ----------------------
  * A 3D U-Net (4 levels, 16/32/64/128 channels, 3x3x3 convolutions, BF16
  * weights and activations, FP32 accumulation, tensor-core implicit-GEMM

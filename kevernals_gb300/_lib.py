@@ -72,6 +72,9 @@ SIGNATURES = {
     "kv_plan_set_slab": ([_vp, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "kv_plan_get_back_shape": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "kv_plan_set_back_shape": ([_vp, C.c_int, C.c_int], C.c_int),
+    "kv_plan_get_back_staging": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)], C.c_int),
+    "kv_plan_set_back_staging": ([_vp, C.c_int, C.c_int], C.c_int),
     "kv_warm_ratio": ([_vp, _vp, _vp, _vp, C.c_size_t, C.POINTER(C.c_double)], C.c_int),
     "kv_warm_normalize": ([_vp, _vp, _vp, _vp, C.c_size_t], C.c_int),
     "kv_warm_fill": ([_vp, _vp, _vp, _vp, C.c_float, _vp, C.c_size_t], C.c_int),

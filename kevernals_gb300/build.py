@@ -26,6 +26,7 @@ SOURCES = {
     "kv_rc.cu": ["-fmad=false"],
     "kv_misc.cu": [],
     "kv_fwd_slab.cu": [],
+    "kv_back_stage.cu": [],
     "kv_unet.cu": [],
 }
 

@@ -39,9 +39,10 @@ kv_status device_status(kv_ctx *ctx) {
     KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (h == 0) return KV_OK;
     KV_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
-    return kv_fail(ctx, (h & 1) ? KV_ERR_TIMEOUT : KV_ERR_CUDA,
+    return kv_fail(ctx, (h & 9) ? KV_ERR_TIMEOUT : KV_ERR_CUDA,
                    "a projector kernel stopped early (status bits 0x%x: 1 = a staged load did not arrive, "
-                   "2/4 = a ray left its staged box)", h);
+                   "2/4 = a ray left its staged box, 8 = a staged detector patch did not arrive, "
+                   "16 = a voxel tile's candidates left its staged patch)", h);
 }
 
 kv_status residual_from_red(kv_ctx *ctx, double *res, double *ll) {
@@ -759,7 +760,8 @@ kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float 
                       plan->graph_iters == iters && plan->graph_mlem == (int)mlem && plan->graph_relax == relax &&
                       plan->graph_fb == plan->fwd_by && plan->graph_bb == plan->back_by &&
                       plan->graph_slab == slab_key(plan->fslab) && plan->graph_br == plan->back_rows &&
-                      plan->graph_bs == plan->back_slices;
+                      plan->graph_bs == plan->back_slices &&
+                      plan->graph_bst == plan->bstage.R * 16 + plan->bstage.stages;
     if (!same) {
         if (plan->graph_exec != nullptr) {
             KV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -794,6 +796,7 @@ kv_status iterate_graph(kv_plan *plan, const void *p, void *x, int iters, float 
         plan->graph_slab = slab_key(plan->fslab);
         plan->graph_br = plan->back_rows;
         plan->graph_bs = plan->back_slices;
+        plan->graph_bst = plan->bstage.R * 16 + plan->bstage.stages;
     }
     KV_CHECK_CUDA(ctx, cudaGraphLaunch(plan->graph_exec, ctx->stream));
     return KV_OK;
@@ -1057,6 +1060,32 @@ extern "C" kv_status kv_plan_set_slab(kv_plan *plan, int rays_per_thread, int sl
         return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "slab shape (%d, %d, %d, %d) does not fit: %s",
                        rays_per_thread, slices, stages, view_group, why.c_str());
     plan->fslab = c;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_get_back_staging(const kv_plan *plan, int *rows_per_thread, int *stages,
+                                              int *patch_cols, int *patch_rows) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (rows_per_thread) *rows_per_thread = plan->bstage.R;
+    if (stages) *stages = plan->bstage.stages;
+    if (patch_cols) *patch_cols = plan->bstage.BU;
+    if (patch_rows) *patch_rows = plan->bstage.BV;
+    return KV_OK;
+}
+
+extern "C" kv_status kv_plan_set_back_staging(kv_plan *plan, int rows_per_thread, int stages) {
+    if (plan == nullptr) return KV_ERR_INVALID_ARG;
+    if (rows_per_thread == 0) {
+        plan->bstage = BackStageCfg{};
+        return KV_OK;
+    }
+    if (plan->family != KV_FAMILY_EXACT)
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "the staged backprojector is an EXACT-family kernel");
+    BackStageCfg c;
+    std::string why;
+    if (!back_stage_fit(plan, rows_per_thread, stages, &c, &why))
+        return kv_fail(plan->ctx, KV_ERR_UNSUPPORTED, "%s", why.c_str());
+    plan->bstage = c;
     return KV_OK;
 }
 

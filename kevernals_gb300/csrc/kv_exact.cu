@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 namespace {
 
@@ -719,6 +720,7 @@ kv_status exact_build_tables(kv_plan *plan, const float *src, const float *det, 
         host->yt = std::move(yt);
         host->yi = std::move(yi);
         host->hr = std::move(hr);
+        host->rng = std::move(rng);
     }
     return KV_OK;
 }
@@ -768,6 +770,7 @@ void back_r_dispatch(int R, int S, const ExGeom &G, const ExactTables &t, BackMo
 template <typename VolT, typename ProjT>
 kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan, int z0, int nzs) {
     ExGeom G = exgeom(plan, plan->g.n_views);
+    if (!kahan && plan->bstage.R > 0) return back_stage_launch(plan, mode, a, z0, nzs, plan->g.n_views);
     if (plan->back_rows > 0) {
         LaunchTimer lt(plan->ctx, "exact_back");
         if (kahan) back_r_dispatch<VolT, ProjT, ACC_KAHAN>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
@@ -1216,6 +1219,7 @@ struct TuneResult {
     int fwd_by, back_by;
     FwdSlabCfg fslab;
     int back_rows, back_slices;
+    BackStageCfg bstage;
 };
 
 std::mutex g_tune_mutex;
@@ -1267,9 +1271,27 @@ kv_status tune_shapes(kv_plan *plan, int P, TuneResult &best) {
             exact_back_kernel<VolT, ProjT, ACC, BACK_PLAIN><<<grid, block, 0, ctx->stream>>>(G, plan->ex, ba, nullptr, 0);
         });
         if (ms < bt) {
+            bt = ms;
             best.back_rows = 0;
             best.back_slices = 1;
         }
+    }
+    // the staged backprojector (FP32 storage), used instead when it is faster
+    best.bstage = BackStageCfg{};
+    if constexpr (std::is_same<VolT, float>::value && ACC == ACC_F32) {
+        static const int sshapes[][2] = {{8, 2}, {4, 2}, {4, 3}};
+        const BackStageCfg keep_stage = plan->bstage;
+        for (const auto &sh : sshapes) {
+            BackStageCfg c;
+            if (!back_stage_fit(plan, sh[0], sh[1], &c, nullptr)) continue;
+            plan->bstage = c;
+            const float ms = median3(ctx, e0, e1, [&] { back_stage_launch(plan, BACK_PLAIN, ba, 0, g.nz, P); });
+            if (ms < bt) {
+                bt = ms;
+                best.bstage = c;
+            }
+        }
+        plan->bstage = keep_stage;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1293,6 +1315,7 @@ kv_status exact_autotune(kv_plan *plan) {
         plan->fslab = r.fslab;
         plan->back_rows = r.back_rows;
         plan->back_slices = r.back_slices;
+        plan->bstage = r.bstage;
     };
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -1308,7 +1331,7 @@ kv_status exact_autotune(kv_plan *plan) {
     KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_vol, 0, plan->nvox * es, ctx->stream));
     KV_CHECK_CUDA(ctx, cudaMemsetAsync(plan->d_ratio, 0, plan->nproj * es, ctx->stream));
     const ExGeom G = exgeom(plan, g.n_views < 6 ? g.n_views : 6);
-    TuneResult r{plan->fwd_by, plan->back_by, plan->fslab, plan->back_rows, plan->back_slices};
+    TuneResult r{plan->fwd_by, plan->back_by, plan->fslab, plan->back_rows, plan->back_slices, plan->bstage};
     // one-thread-per-ray / per-voxel block heights (the fallback kernels)
     switch (plan->storage) {
     case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;

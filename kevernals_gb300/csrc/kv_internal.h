@@ -78,7 +78,7 @@ struct ExactTables {
 // Host copies of the same tables (the slab forward projector sizes its
 // shared-memory boxes from them with the kernel's own float arithmetic).
 struct ExactHostTables {
-    std::vector<float4> xt, yt;
+    std::vector<float4> xt, yt, rng;
     std::vector<int> xi, yi;
     std::vector<float> hr;
 };
@@ -94,6 +94,15 @@ struct FwdSlabCfg {
     size_t smem = 0;    // dynamic shared memory per CTA
 };
 
+// Shape of the TMA-staged EXACT backprojector (kv_back_stage.cu, FP32
+// storage); R == 0: the plan uses exact_back_r_kernel / exact_back_kernel.
+struct BackStageCfg {
+    int R = 0;          // voxel rows per thread: a CTA covers 32 x 8R voxels of one slice
+    int stages = 0;     // detector patches in flight
+    int BU = 0, BV = 0; // patch extent in detector columns / rows
+    size_t smem = 0;    // dynamic shared memory per CTA
+};
+
 struct kv_plan {
     kv_ctx *ctx = nullptr;
     kv_geometry g{};
@@ -106,6 +115,7 @@ struct kv_plan {
     ExactTables ex;                  // EXACT family
     ExactHostTables hx;              // host copies of ex
     FwdSlabCfg fslab;                // slab forward projector (R == 0: not used)
+    BackStageCfg bstage;             // staged backprojector (R == 0: not used)
     float *d_src = nullptr;          // RC family: [P][3] sources (float3 layout)
     float *d_org = nullptr;          // RC family: [P][3] detector origins
 
@@ -132,7 +142,7 @@ struct kv_plan {
     const void *graph_x = nullptr;
     int graph_iters = 0, graph_mlem = 0, graph_fb = 0, graph_bb = 0;
     long long graph_slab = 0;
-    int graph_br = 0, graph_bs = 0;
+    int graph_br = 0, graph_bs = 0, graph_bst = 0;
     float graph_relax = 0.f;
 };
 
@@ -274,6 +284,15 @@ int fwd_slab_default_group(int n_views);
 size_t fwd_slab_blocks(const kv_plan *plan, int n_views);
 kv_status fwd_slab_launch(kv_plan *plan, const ExactTables &t, int n_views, FwdMode mode, const FwdArgs &a,
                           double *partials);
+
+// TMA-staged EXACT backprojector (kv_back_stage.cu): back_stage_fit checks
+// that the plan suits it (FP32 storage, 16-byte detector rows, every
+// voxel tile's view of the detector within 256 x 256 pixels and the
+// shared-memory budget) and sizes the patch for (R, stages);
+// back_stage_launch runs slices [z0, z0 + nzs) over the plan's first n_views
+// views (all of them outside the autotuner).
+bool back_stage_fit(const kv_plan *plan, int R, int stages, BackStageCfg *out, std::string *why);
+kv_status back_stage_launch(kv_plan *plan, BackMode mode, const BackArgs &a, int z0, int nzs, int n_views);
 
 // RC driver epilogue modes (forward: ratio / residual fused; back: update fused)
 enum RcMode : int { RC_PLAIN = 0, RC_MLEM = 1, RC_ART = 2 };

@@ -361,8 +361,22 @@ def _plan_set_back_shape(self, rows_per_thread, slices_per_thread=1):
     self.ctx.check(lib().kv_plan_set_back_shape(self._h, int(rows_per_thread), int(slices_per_thread)))
 
 
+def _plan_back_staging(self):
+    """(voxel rows per thread, stages, patch columns, patch rows) of the
+    TMA-staged backprojector; rows 0: not used."""
+    v = [C.c_int() for _ in range(4)]
+    self.ctx.check(lib().kv_plan_get_back_staging(self._h, *[C.byref(x) for x in v]))
+    return tuple(x.value for x in v)
+
+
+def _plan_set_back_staging(self, rows_per_thread, stages=2):
+    self.ctx.check(lib().kv_plan_set_back_staging(self._h, int(rows_per_thread), int(stages)))
+
+
 Plan.back_shape = property(_plan_back_shape)
 Plan.set_back_shape = _plan_set_back_shape
+Plan.back_staging = property(_plan_back_staging)
+Plan.set_back_staging = _plan_set_back_staging
 Plan.slab = property(_plan_slab)
 Plan.set_slab = _plan_set_slab
 Plan.autotune = _plan_autotune

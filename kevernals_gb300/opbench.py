@@ -54,6 +54,8 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--back-shape", default="",
                     help="gather backprojector: rows,slices per thread (rows 0: one voxel per thread)")
+    ap.add_argument("--back-staging", default="",
+                    help="TMA-staged backprojector: rows,stages (rows 0: off)")
     ap.add_argument("--slab", default="",
                     help="forward projector shape: 'off' (one thread per ray) or R,S,stages,group")
     args = ap.parse_args(argv)
@@ -96,6 +98,8 @@ def main(argv=None):
                 plans[family].set_slab(*shape)
             if family == "exact" and args.back_shape:
                 plans[family].set_back_shape(*[int(v) for v in args.back_shape.split(",")])
+            if family == "exact" and args.back_staging:
+                plans[family].set_back_staging(*[int(v) for v in args.back_staging.split(",")])
         return plans[family]
 
     p = plan("exact").forward(truth)

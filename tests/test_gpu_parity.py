@@ -454,6 +454,63 @@ def test_back_shapes_bit_identical(ctx):
         plan.close()
 
 
+def test_back_staging_bit_identical(ctx):
+    """The TMA-staged backprojector (each view's detector patch in shared
+    memory, one view ahead) against the gather kernel: identical volumes for
+    the plain backprojection and after MLEM / SART iterations (fused
+    updates), on every geometry whose detector rows are a whole number of 16
+    bytes; the others (nu = 37) are refused, as are 16-bit storage and bad
+    shapes.  The last geometry's detector rows are 20 times finer than its
+    voxel rows (up to 25 candidate rows per voxel row: several fill passes)
+    and its 88 x 244 patches leave room for two stages only."""
+    torch = pytest.importorskip("torch")
+    fine_rows = linear_sweep(24, 12, 6, 1.0, 1.0, 1.0, 5, 96, 256, 0.3, 0.05, 15.0)
+    staged = 0
+    for gi, g in enumerate(small_geoms() + [fine_rows]):
+        y = np.random.default_rng(4).random(g.proj_shape, dtype=np.float32)
+        plan = engine.Plan(ctx, g, "exact")
+        ref = plan.back(y)
+        p = O.exact_forward(g, phantom_for(g).astype(np.float64)).astype(np.float32)
+        pd = torch.from_numpy(p).cuda()
+        runs = {}
+        for shape in [(0, 2), (4, 2), (8, 2), (4, 3)]:
+            if shape[0]:
+                try:
+                    plan.set_back_staging(*shape)
+                except KvError:
+                    assert g.nu % 4 != 0 or (gi == 3 and shape == (4, 3)), (gi, shape)
+                    continue
+                staged += 1
+                assert plan.back_staging[:2] == shape
+                assert np.array_equal(plan.back(y), ref), shape
+            else:
+                plan.set_back_staging(0)
+            out = []
+            for method, relax, x0 in (("mlem", 1.0, 1.0), ("sart", 0.5, 0.0)):
+                x = torch.full(g.volume_shape, x0, dtype=torch.float32, device="cuda")
+                getattr(plan, method)(pd, x, 3, relax)
+                torch.cuda.synchronize()
+                out.append(x.cpu().numpy())
+            runs[shape] = out
+        for shape, out in runs.items():
+            for a, b in zip(out, runs[(0, 2)]):
+                assert np.array_equal(a, b), shape
+        plan.set_back_staging(0)
+        assert plan.back_staging[0] == 0
+        plan.close()
+    assert staged == 8
+    g = small_geoms()[0]
+    plan = engine.Plan(ctx, g, "exact", "bf16")
+    with pytest.raises(KvError):
+        plan.set_back_staging(4, 2)
+    plan.close()
+    plan = engine.Plan(ctx, g, "exact")
+    for bad in [(2, 2), (4, 1), (4, 4)]:
+        with pytest.raises(KvError):
+            plan.set_back_staging(*bad)
+    plan.close()
+
+
 def test_exact_config1_full_size_vs_fp64(ctx):
     """The whole config-1 workload (256x256x64 voxels, 15 views of 512^2):
     the forward projection of its seeded 40-ellipsoid phantom and the
