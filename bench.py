@@ -32,6 +32,7 @@ value = all ranks' rays / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -227,7 +228,10 @@ def reference_cpu_steps(g, truth, steps, warmup, seconds=None, fraction=None, se
     forward(truth, rays, p)                          # the sampled rays' measurements
     for _ in range(warmup):
         step(rays, vox)
+    gc.collect()
+    gc.disable()                       # as in the GPU arm's timed loops
     times = [step(rays, vox) for _ in range(steps)]
+    gc.enable()
     units = len(rays) + len(vox) * g.n_rays / g.n_voxels     # rays, and voxels in ray units
     what = ("the reference's Projector.cu kernels compiled for the host (OpenMP)" if use_ref
             else "the oracle's restatement of the reference kernels (selection sort, 11x11 window; OpenMP)")
@@ -501,12 +505,17 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- timed region: device-resident inputs (both larger than L2)
+    # ---- timed region: device-resident inputs (both larger than L2).  As in
+    # timeit, Python's garbage collector is run before and held off during
+    # the timed loops: its pauses between two calls of the C ABI would idle
+    # the GPU (measured: periodic 5-15 ms stalls of the host-buffer loop).
     sampler = ClockSampler(dev)
     sampler.start()
     ctx.set_timing(True)
     barrier()
     torch.cuda.synchronize()
+    gc.collect()
+    gc.disable()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -514,6 +523,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
         plan.mlem(p, x, 1)
     e1.record(stream)
     torch.cuda.synchronize()
+    gc.enable()
     barrier()
     ms = e0.elapsed_time(e1)
     kernels = ctx.read_timing()
@@ -550,6 +560,8 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
         plan.mlem(hp, hx, 1)          # warm the staging buffers
         barrier()
         torch.cuda.synchronize()
+        gc.collect()
+        gc.disable()
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(stream)
@@ -557,6 +569,7 @@ def gpu_arm(args, g, n_ell, i0, cfg, desc, rank, world):
             plan.mlem(hp, hx, 1)
         a1.record(stream)
         torch.cuda.synchronize()
+        gc.enable()
         barrier()
         ems = max_over_ranks(a0.elapsed_time(a1), world, f"cuda:{dev}")
         e2e = {"value": world * rays_per_step * args.steps / (ems * 1e-3), "unit": UNIT,
