@@ -281,11 +281,13 @@ __global__ void prescale_kernel(ExGeom G, ExactTables T, const float *y, ProjT *
 // (Computing the x-intervals once per block in shared memory instead -- they
 // depend on the column, not the row -- measured slower: the two block
 // barriers per view cost more than the redundant interval arithmetic.)
-// Accumulators of the backprojector: plain FP32, Kahan-compensated FP32 (the
-// reduced-precision storage modes), and a double-float sum of exact products
+// Accumulators of the backprojector: plain FP32 (every storage mode: with
+// 16-bit ratio images and volumes, their rounding dominates; a compensated
+// sum measured the same errors to three digits after 50 MLEM iterations and
+// cost a quarter of the iteration), and a double-float sum of exact products
 // (TwoProduct + TwoSum in FP32 arithmetic, ~1e-14 relative) for the FP64
 // sensitivity image.
-enum { ACC_F32 = 0, ACC_KAHAN = 1, ACC_DF = 2 };
+enum { ACC_F32 = 0, ACC_DF = 2 };
 
 // Candidate detector columns a lane holds in registers at once (a voxel at
 // the chest-DT geometry has 4-7).
@@ -294,12 +296,7 @@ constexpr int BACK_SLOTS = 8;
 // One backprojection term w * y into the accumulator (acc, comp).
 template <int ACC>
 __device__ __forceinline__ void back_accumulate(float w, float yv, float &acc, float &comp) {
-    if (ACC == ACC_KAHAN) {         // compensated (Kahan) summation
-        const float y_ = __fsub_rn(__fmul_rn(w, yv), comp);
-        const float t_ = __fadd_rn(acc, y_);
-        comp = __fsub_rn(__fsub_rn(t_, acc), y_);
-        acc = t_;
-    } else if (ACC == ACC_DF) {     // exact product + TwoSum: a double-float sum
+    if (ACC == ACC_DF) {            // exact product + TwoSum: a double-float sum
         const float pr = __fmul_rn(w, yv);
         const float pe = __fmaf_rn(w, yv, -pr);
         const float s_ = __fadd_rn(acc, pr);
@@ -768,13 +765,13 @@ void back_r_dispatch(int R, int S, const ExGeom &G, const ExactTables &t, BackMo
 }
 
 template <typename VolT, typename ProjT>
-kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool kahan, int z0, int nzs) {
+kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, int z0, int nzs) {
     ExGeom G = exgeom(plan, plan->g.n_views);
-    if (!kahan && plan->bstage.R > 0) return back_stage_launch(plan, mode, a, z0, nzs, plan->g.n_views);
+    if (std::is_same<VolT, float>::value && plan->bstage.R > 0)
+        return back_stage_launch(plan, mode, a, z0, nzs, plan->g.n_views);
     if (plan->back_rows > 0) {
         LaunchTimer lt(plan->ctx, "exact_back");
-        if (kahan) back_r_dispatch<VolT, ProjT, ACC_KAHAN>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
-        else back_r_dispatch<VolT, ProjT, ACC_F32>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
+        back_r_dispatch<VolT, ProjT, ACC_F32>(plan->back_rows, plan->back_slices, G, plan->ex, mode, a, nullptr, z0, nzs, plan->ctx->stream);
         KV_CHECK_LAUNCH(plan->ctx, "exact_back_r_kernel");
         return KV_OK;
     }
@@ -783,18 +780,10 @@ kv_status back_dispatch(kv_plan *plan, BackMode mode, const BackArgs &a, bool ka
     cudaStream_t st = plan->ctx->stream;
     const ExactTables &t = plan->ex;
     LaunchTimer lt(plan->ctx, "exact_back");
-    if (kahan) {
-        switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_KAHAN, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        }
-    } else {
-        switch (mode) {
-        case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
-        }
+    switch (mode) {
+    case BACK_PLAIN: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_PLAIN><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+    case BACK_MLEM: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_MLEM><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
+    case BACK_SART: exact_back_kernel<VolT, ProjT, ACC_F32, BACK_SART><<<grid, block, 0, st>>>(G, t, a, nullptr, z0); break;
     }
     KV_CHECK_LAUNCH(plan->ctx, "exact_back_kernel");
     return KV_OK;
@@ -858,9 +847,9 @@ kv_status exact_back_slab_launch(kv_plan *plan, BackMode mode, const BackArgs &a
     if (z0 < 0 || nzs < 1 || z0 + nzs > plan->g.nz)
         return kv_fail(plan->ctx, KV_ERR_INVALID_ARG, "bad slice range for the backprojection");
     switch (plan->storage) {
-    case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, true, z0, nzs);
-    case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, true, z0, nzs);
-    default: return back_dispatch<float, float>(plan, mode, a, false, z0, nzs);
+    case KV_STORAGE_BF16: return back_dispatch<__nv_bfloat16, __nv_bfloat16>(plan, mode, a, z0, nzs);
+    case KV_STORAGE_F16: return back_dispatch<__half, __half>(plan, mode, a, z0, nzs);
+    default: return back_dispatch<float, float>(plan, mode, a, z0, nzs);
     }
 }
 
@@ -1334,8 +1323,8 @@ kv_status exact_autotune(kv_plan *plan) {
     TuneResult r{plan->fwd_by, plan->back_by, plan->fslab, plan->back_rows, plan->back_slices, plan->bstage};
     // one-thread-per-ray / per-voxel block heights (the fallback kernels)
     switch (plan->storage) {
-    case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
-    case KV_STORAGE_F16: tune<__half, __half, ACC_KAHAN>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
+    case KV_STORAGE_BF16: tune<__nv_bfloat16, __nv_bfloat16, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
+    case KV_STORAGE_F16: tune<__half, __half, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
     default: tune<float, float, ACC_F32>(ctx, G, plan->ex, plan->d_vol, plan->d_ratio, r.fwd_by, r.back_by); break;
     }
     cudaError_t e = cudaGetLastError();
@@ -1343,8 +1332,8 @@ kv_status exact_autotune(kv_plan *plan) {
     // slab forward and gather backprojector shapes
     const int P = g.n_views < 12 ? g.n_views : 12;
     switch (plan->storage) {
-    case KV_STORAGE_BF16: KV_TRY((tune_shapes<__nv_bfloat16, __nv_bfloat16, ACC_KAHAN>(plan, P, r))); break;
-    case KV_STORAGE_F16: KV_TRY((tune_shapes<__half, __half, ACC_KAHAN>(plan, P, r))); break;
+    case KV_STORAGE_BF16: KV_TRY((tune_shapes<__nv_bfloat16, __nv_bfloat16, ACC_F32>(plan, P, r))); break;
+    case KV_STORAGE_F16: KV_TRY((tune_shapes<__half, __half, ACC_F32>(plan, P, r))); break;
     default: KV_TRY((tune_shapes<float, float, ACC_F32>(plan, P, r))); break;
     }
     apply(r);

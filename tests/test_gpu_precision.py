@@ -1,7 +1,7 @@
 """Mixed precision at the 256x256x64 / 15 x 512^2 workload: 50 MLEM
 iterations with the volume and projections stored in FP32, BF16 and FP16
-(FP32 path-length accumulation, Kahan-compensated backprojection sums, FP64
-sensitivity and reductions), against the FP64 oracle MLEM and against FP32
+(FP32 path-length and backprojection accumulation, FP64 sensitivity and
+reductions), against the FP64 oracle MLEM and against FP32
 GPU MLEM.  The measured errors are printed; the bounds below are the stated
 tolerances."""
 import json
